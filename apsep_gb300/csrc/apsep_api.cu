@@ -1,0 +1,273 @@
+// apsep_api.cu -- the C ABI (include/apsep.h): plans, runs, status codes.
+//
+// A plan owns one device allocation of scratch (control block, look-back
+// status words, tile mins, chunk mins) sized for its capacity; runs only
+// enqueue kernels.  Errors are status codes, never exit() (the reference's
+// gpuAssert exits, src/apsep.cuh:39-47).
+#include <cudaTypedefs.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "apsep.h"
+#include "apsep_internal.h"
+
+using namespace apsep;
+
+struct apsep_plan {
+    int device = 0;
+    int dtype = 0;
+    int cmp = 0;
+    int cfg = 0;
+    int64_t capacity = 0;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    TileScratch ts{};
+    int dbg_skip_tile = -1;
+    uint32_t dbg_spin_limit = 0;
+};
+
+namespace {
+
+constexpr uint32_t kDefaultSpinLimit = 1u << 22;  // ~1 s of polling with back-off
+constexpr int kMinTileKeys = 2048;               // smallest tile of kTileConfigs
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+    std::call_once(g_encode_once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    });
+    return g_encode;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// 2-D view of n keys as rows of 32 (128 bytes), box = one tile.
+bool encode_rows(CUtensorMap* map, const void* base, int rows, int tile_rows, int dtype) {
+    auto enc = encoder();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {32, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {128};
+    cuuint32_t box[2] = {32, (cuuint32_t)tile_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, dtype == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_INT32, 2,
+                     const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            ok = false;
+            return;
+        }
+        if (prev != dev && cudaSetDevice(dev) != cudaSuccess) ok = false;
+    }
+    ~DeviceGuard() {
+        int cur;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+bool ranges_overlap(const void* a, size_t an, const void* b, size_t bn) {
+    uintptr_t a0 = (uintptr_t)a, b0 = (uintptr_t)b;
+    return a0 < b0 + bn && b0 < a0 + an;
+}
+
+}  // namespace
+
+extern "C" {
+
+int apsep_version(void) { return 10000; }
+
+const char* apsep_status_string(apsep_status s) {
+    switch (s) {
+    case APSEP_OK: return "ok";
+    case APSEP_EINVAL: return "invalid argument";
+    case APSEP_ENOMEM: return "out of device memory";
+    case APSEP_ECUDA: return "CUDA error";
+    case APSEP_ETIMEOUT: return "device-side wait timed out";
+    case APSEP_EINTERNAL: return "device-side invariant failed";
+    case APSEP_ENOTSUP: return "not supported";
+    }
+    return "unknown status";
+}
+
+int32_t apsep_num_configs(void) { return kNumTileConfigs; }
+
+apsep_status apsep_config_shape(int32_t config, int32_t* threads, int32_t* keys_per_thread) {
+    if (config < 0 || config >= kNumTileConfigs) return APSEP_EINVAL;
+    if (threads) *threads = kTileConfigs[config].nt;
+    if (keys_per_thread) *keys_per_thread = kTileConfigs[config].ipt;
+    return APSEP_OK;
+}
+
+apsep_status apsep_plan_create(apsep_plan** out, apsep_dtype dtype, apsep_cmp cmp, int64_t capacity) {
+    if (!out) return APSEP_EINVAL;
+    *out = nullptr;
+    if ((dtype != APSEP_INT32 && dtype != APSEP_FLOAT32) || (cmp != APSEP_LT && cmp != APSEP_LE))
+        return APSEP_EINVAL;
+    if (capacity < 0 || capacity > (int64_t)INT32_MAX) return APSEP_EINVAL;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return APSEP_ECUDA;
+    int major = 0;
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess) return APSEP_ECUDA;
+    if (major < 10) return APSEP_ENOTSUP;  // TMA tensor path + sm_103a build
+
+    apsep_plan* p = new apsep_plan();
+    p->device = dev;
+    p->dtype = dtype;
+    p->cmp = cmp;
+    p->capacity = capacity;
+    const int64_t cap = capacity > 0 ? capacity : 1;
+    const int64_t cap_tiles = (cap + kMinTileKeys - 1) / kMinTileKeys + 1;
+    const size_t off_state = align_up(sizeof(Counters), 256);
+    const size_t off_tmin = align_up(off_state + (size_t)cap_tiles * 8, 256);
+    const size_t off_cmin = align_up(off_tmin + (size_t)cap_tiles * 4, 256);
+    // chunk mins: num_tiles * tile/32 <= cap/32 + tile/32 for every tile size <= 8192
+    const size_t cmin_entries = (size_t)(cap + 31) / 32 + 8192 / 32;
+    const size_t total = align_up(off_cmin + cmin_entries * 4, 256);
+    if (cudaMalloc(&p->scratch, total) != cudaSuccess) {
+        cudaGetLastError();
+        delete p;
+        return APSEP_ENOMEM;
+    }
+    p->scratch_bytes = total;
+    char* base = (char*)p->scratch;
+    p->ts.ctr = (Counters*)base;
+    p->ts.state = (uint64_t*)(base + off_state);
+    p->ts.tile_min = base + off_tmin;
+    p->ts.chunk_min = base + off_cmin;
+    p->ts.cap_tiles = (int)cap_tiles;
+    Counters c0;
+    memset(&c0, 0, sizeof(c0));
+    c0.epoch = 1;
+    if (cudaMemset(p->scratch, 0, total) != cudaSuccess ||
+        cudaMemcpy(p->ts.ctr, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(p->scratch);
+        delete p;
+        return APSEP_ECUDA;
+    }
+    for (int cfg = 0; cfg < kNumTileConfigs; cfg++)
+        if (single_prepare(cfg) != cudaSuccess) {
+            cudaFree(p->scratch);
+            delete p;
+            return APSEP_ECUDA;
+        }
+    *out = p;
+    return APSEP_OK;
+}
+
+apsep_status apsep_plan_destroy(apsep_plan* p) {
+    if (!p) return APSEP_OK;
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaFree(p->scratch);
+    delete p;
+    return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
+}
+
+apsep_status apsep_plan_get_info(const apsep_plan* p, apsep_plan_info* info) {
+    if (!p || !info) return APSEP_EINVAL;
+    memset(info, 0, sizeof(*info));
+    info->capacity = p->capacity;
+    info->scratch_bytes = (int64_t)p->scratch_bytes;
+    info->tile_keys = kTileConfigs[p->cfg].nt * kTileConfigs[p->cfg].ipt;
+    info->config = p->cfg;
+    info->device = p->device;
+    info->dtype = p->dtype;
+    info->cmp = p->cmp;
+    return APSEP_OK;
+}
+
+apsep_status apsep_plan_set_config(apsep_plan* p, int32_t config) {
+    if (!p || config < 0 || config >= kNumTileConfigs) return APSEP_EINVAL;
+    p->cfg = config;
+    return APSEP_OK;
+}
+
+apsep_status apsep_run_cmp(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                           void* stream) {
+    if (!p || n < 0 || (cmp != APSEP_LT && cmp != APSEP_LE)) return APSEP_EINVAL;
+    if (n == 0) return APSEP_OK;
+    if (n > p->capacity || !d_in || !d_out) return APSEP_EINVAL;
+    if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_EINVAL;
+    DeviceGuard g(p->device);
+    if (!g.ok) return APSEP_ECUDA;
+
+    const TileConfig tc = kTileConfigs[p->cfg];
+    const int B = tc.nt * tc.ipt;
+    const int tile_rows = B / 32;
+    const int64_t num_tiles = (n + B - 1) / B;
+    int rows = (int)(n / 32);
+    CUtensorMap mi, mo;
+    memset(&mi, 0, sizeof(mi));
+    memset(&mo, 0, sizeof(mo));
+    const bool aligned = ((uintptr_t)d_in % 16 == 0) && ((uintptr_t)d_out % 16 == 0);
+    if (!aligned || rows < tile_rows) rows = 0;
+    if (rows > 0) {
+        if (!encode_rows(&mi, d_in, rows, tile_rows, p->dtype) || !encode_rows(&mo, d_out, rows, tile_rows, 0))
+            return APSEP_ECUDA;
+    }
+    SingleArgs a;
+    a.d_in = d_in;
+    a.d_out = d_out;
+    a.n = (int)n;
+    a.num_tiles = (int)num_tiles;
+    a.tma_rows = rows;
+    a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
+    a.skip_publish_tile = p->dbg_skip_tile;
+    a.s = p->ts;
+    p->dbg_skip_tile = -1;  // one-shot
+    p->dbg_spin_limit = 0;
+    cudaError_t e = launch_single(p->dtype, cmp == APSEP_LE ? 1 : 0, p->cfg, a, mi, mo, (cudaStream_t)stream);
+    return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
+}
+
+apsep_status apsep_run(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n, void* stream) {
+    if (!p) return APSEP_EINVAL;
+    return apsep_run_cmp(p, d_in, d_out, n, (apsep_cmp)p->cmp, stream);
+}
+
+apsep_status apsep_plan_check(apsep_plan* p, void* stream) {
+    if (!p) return APSEP_EINVAL;
+    DeviceGuard g(p->device);
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return APSEP_ECUDA;
+    uint32_t err = 0;
+    if (cudaMemcpy(&err, &p->ts.ctr->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return APSEP_ECUDA;
+    if (!err) return APSEP_OK;
+    uint32_t zero = 0;
+    if (cudaMemcpy(&p->ts.ctr->err, &zero, 4, cudaMemcpyHostToDevice) != cudaSuccess) return APSEP_ECUDA;
+    if (err & (ERR_LOOKBACK_TIMEOUT | ERR_TMA_TIMEOUT)) return APSEP_ETIMEOUT;
+    return APSEP_EINTERNAL;
+}
+
+apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp) {
+    if (n == 0) return APSEP_OK;
+    apsep_plan* p = nullptr;
+    apsep_status s = apsep_plan_create(&p, dtype, cmp, n);
+    if (s != APSEP_OK) return s;
+    s = apsep_run(p, d_in, d_out, n, nullptr);
+    apsep_status c = apsep_plan_check(p, nullptr);
+    apsep_plan_destroy(p);
+    return s != APSEP_OK ? s : c;
+}
+
+apsep_status apsep_debug_inject(apsep_plan* p, int32_t tile, uint32_t spin_limit) {
+    if (!p || tile < -1) return APSEP_EINVAL;
+    p->dbg_skip_tile = tile;
+    p->dbg_spin_limit = spin_limit;
+    return APSEP_OK;
+}
+
+}  // extern "C"

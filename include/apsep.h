@@ -1,0 +1,123 @@
+/*
+ * apsep.h -- C ABI of the GB300-native APSE engine (libapsep.so).
+ *
+ * All Previous Smaller Element: for each key a[i], out[i] is the largest
+ * j < i with a[j] < a[i] (APSEP_LT) or a[j] <= a[i] (APSEP_LE), else -1.
+ * Keys are int32 or float32 (finite: NaN keys are outside the contract),
+ * outputs are int32 indices, so n < 2^31.
+ *
+ * Plain pointers and sizes only: device pointers from any allocator
+ * (cudaMalloc, torch), `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  No call exits the process; every failure is an
+ * apsep_status.
+ *
+ * Reference interfaces each entry point replaces (CoderDue/APSEP,
+ * src/apsep.cuh):
+ *   apsep_plan_create   allocSPTScratch<T,BS,IPT,INCL>(n)   src/apsep.cuh:3014-3040
+ *                       allocWSTLScratch<T,BS,IPT>(n)       src/apsep.cuh:2521-2537
+ *   apsep_plan_destroy  freeSPTScratch(s)                   src/apsep.cuh:3042-3050
+ *                       freeWSTLScratch(s)                  src/apsep.cuh:2539-2546
+ *   apsep_run           runSPT<T,BS,IPT,INCL>(d_in,d_out,n,s)  src/apsep.cuh:3052-3067
+ *                       runWSTL<T,BS,IPT>(d_in,d_out,n,s)   src/apsep.cuh:2548-2596
+ *   apsep_run_cmp       runSPT<...,INCL> with the comparator chosen per call
+ *                       (the INCL template argument, src/apsep.cuh:2669-2673)
+ *   apsep_launch        launchSPT / launchWSTL: alloc + run + sync + free
+ *                       src/apsep.cuh:3069-3076, 2598-2605
+ *   apsep_plan_check    gpuAssert after a sync (src/apsep.cuh:39-47), but
+ *                       returning a status instead of exit()
+ * The C++ shim include/apsep.cuh re-exports the reference template names on
+ * top of these.
+ */
+#ifndef APSEP_H_
+#define APSEP_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum apsep_status {
+    APSEP_OK = 0,
+    APSEP_EINVAL = 1,    /* bad argument: null, n < 0, n > capacity, overlap */
+    APSEP_ENOMEM = 2,    /* device allocation failed */
+    APSEP_ECUDA = 3,     /* a CUDA runtime/driver call failed */
+    APSEP_ETIMEOUT = 4,  /* a bounded device-side wait gave up (see plan_check) */
+    APSEP_EINTERNAL = 5, /* a device-side invariant check failed */
+    APSEP_ENOTSUP = 6    /* unsupported dtype / device */
+} apsep_status;
+
+typedef enum apsep_dtype { APSEP_INT32 = 0, APSEP_FLOAT32 = 1 } apsep_dtype;
+
+typedef enum apsep_cmp {
+    APSEP_LT = 0, /* strict previous-smaller (the reference's INCL=false) */
+    APSEP_LE = 1  /* previous-smaller-or-equal (INCL=true)                */
+} apsep_cmp;
+
+typedef struct apsep_plan apsep_plan;
+
+typedef struct apsep_plan_info {
+    int64_t capacity;       /* largest n a run may use                      */
+    int64_t scratch_bytes;  /* device scratch owned by the plan             */
+    int32_t tile_keys;      /* keys per tile of the selected configuration  */
+    int32_t config;         /* index of the selected kernel configuration   */
+    int32_t device;         /* CUDA device the plan lives on                */
+    int32_t dtype;
+    int32_t cmp;
+    int32_t reserved;
+} apsep_plan_info;
+
+/* Version of this ABI (major*10000 + minor*100 + patch). */
+int apsep_version(void);
+
+/* Human-readable name of a status code (static string). */
+const char* apsep_status_string(apsep_status s);
+
+/* Create a plan for up to `capacity` keys on the current CUDA device.  Owns
+ * all scratch; runs never allocate.  (allocSPTScratch / allocWSTLScratch) */
+apsep_status apsep_plan_create(apsep_plan** plan, apsep_dtype dtype, apsep_cmp cmp, int64_t capacity);
+
+/* Free the plan and its scratch.  Null is a no-op.  (freeSPTScratch) */
+apsep_status apsep_plan_destroy(apsep_plan* plan);
+
+/* Enqueue one run on `stream`: d_out[0..n) <- APSE(d_in[0..n)).  Asynchronous,
+ * no allocation, no synchronisation, so it can be captured in a CUDA graph.
+ * n == 0 is a no-op.  d_in/d_out need no particular alignment (16-byte
+ * aligned arrays take the TMA path).  Runs on one plan must not overlap in
+ * time (serialise them on one stream).  (runSPT / runWSTL) */
+apsep_status apsep_run(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, void* stream);
+
+/* apsep_run with the comparator chosen per call (runSPT<...,INCL>). */
+apsep_status apsep_run_cmp(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                           void* stream);
+
+/* Synchronise `stream` and report device-side errors of earlier runs on this
+ * plan (APSEP_ETIMEOUT / APSEP_EINTERNAL), clearing them. */
+apsep_status apsep_plan_check(apsep_plan* plan, void* stream);
+
+/* Plan facts (capacity, scratch bytes, tile size, configuration). */
+apsep_status apsep_plan_get_info(const apsep_plan* plan, apsep_plan_info* info);
+
+/* Select a kernel configuration (autotuner hook); 0 <= config < apsep_num_configs(). */
+apsep_status apsep_plan_set_config(apsep_plan* plan, int32_t config);
+int32_t apsep_num_configs(void);
+/* threads per CTA and keys per thread of a configuration */
+apsep_status apsep_config_shape(int32_t config, int32_t* threads, int32_t* keys_per_thread);
+
+/* One-shot: plan, run on the legacy default stream, synchronise, free.
+ * (launchSPT / launchWSTL) */
+apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp);
+
+/* Fault injection for failure-detection tests: the next run's tile `tile`
+ * never publishes its look-back status, and every device wait gives up after
+ * `spin_limit` polls, so its successors report APSEP_ETIMEOUT through
+ * apsep_plan_check instead of hanging.  tile = -1 restores normal runs
+ * (spin_limit 0 = default). */
+apsep_status apsep_debug_inject(apsep_plan* plan, int32_t tile, uint32_t spin_limit);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* APSEP_H_ */

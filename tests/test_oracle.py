@@ -1,0 +1,100 @@
+"""The CPU oracle, pinned against the reference's own outputs.
+
+The golden fixtures (tests/golden/reference_vectors.json) were produced by
+running the reference's cpuApsep (src/main.cu:102-113) and cpuPSE
+(src/bench_spt_le.cu:24-35), compiled from the reference sources, on the
+reference harnesses' own inputs (tests/golden/gen_golden.py).  These tests
+re-derive the same inputs from the same PRNG streams and check the oracle
+restatement bit-exactly against them.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<i4").tobytes()).hexdigest()
+
+
+def test_small_cases_match_reference(golden):
+    cases = golden["main_small_cases"]["cases"]
+    assert len(cases) == 10
+    for c in cases:
+        a = np.asarray(c["input"], dtype=np.int32)
+        assert oracle.apse(a).tolist() == c["expected"], c["label"]
+
+
+@pytest.mark.parametrize("run_idx", [0, 1, 2, 3])
+def test_stress_match_reference(golden, run_idx):
+    run = golden["main_stress"]["runs"][run_idx]
+    rows = run["trials_n_sha256"]
+    for (n, h), a in zip(rows, oracle.main_stress_inputs(run["seed"], run["trials"], run["max_n"])):
+        assert a.shape[0] == n
+        assert sha(oracle.apse(a)) == h
+
+
+def test_spt_le_cases_match_reference(golden):
+    entries = golden["spt_le_cases"]["entries"]
+    full = {}
+    for e in entries:
+        if e["n"] > 1000003:
+            continue  # the 2^25 entries are exercised by the GPU tests
+        name = e["case"]
+        if name not in full:
+            full[name] = oracle.gen_spt_le_case(name, 1000003)
+        a = full[name][: e["n"]]
+        r = oracle.apse(a, e["le"])
+        assert sha(r) == e["sha256"], (name, e["n"], e["le"])
+        for i, want in e["samples"]:
+            assert r[i] == want
+
+
+def test_closed_forms():
+    n = 10000
+    asc = np.arange(n, dtype=np.int32)
+    assert np.array_equal(oracle.apse(asc), np.arange(-1, n - 1, dtype=np.int32))
+    desc = asc[::-1].copy()
+    assert (oracle.apse(desc) == -1).all()
+    eq = np.full(n, 7, np.int32)
+    assert (oracle.apse(eq) == -1).all()
+    assert np.array_equal(oracle.apse(eq, le=True), np.arange(-1, n - 1, dtype=np.int32))
+    assert oracle.apse(np.zeros(0, np.int32)).shape == (0,)
+
+
+def test_float_oracle_matches_definition():
+    rng = np.random.default_rng(5)
+    a = (rng.integers(-50, 50, 3000).astype(np.float32) * np.float32(0.5))
+    a[::7] = -0.0
+    a[::11] = 0.0
+    for le in (False, True):
+        r = oracle.apse(a, le)
+        for i in range(0, a.shape[0], 37):
+            cand = [j for j in range(i) if (a[j] <= a[i] if le else a[j] < a[i])]
+            assert r[i] == (cand[-1] if cand else -1)
+
+
+def test_segmented_oracle():
+    rng = np.random.default_rng(9)
+    lens = rng.integers(0, 300, 50)
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    a = rng.integers(0, 100, int(offs[-1])).astype(np.int32)
+    r = oracle.apse_segmented(a, offs)
+    for s in range(50):
+        lo, hi = offs[s], offs[s + 1]
+        assert np.array_equal(r[lo:hi], oracle.apse(a[lo:hi]))
+
+
+def test_oracle_matches_reference_binary_random():
+    if not oracle.ref_available():
+        pytest.skip("reference tree not present: pinned through the golden fixtures instead")
+    rng = np.random.default_rng(123)
+    for n in (1, 2, 31, 513, 65537):
+        a = rng.integers(0, 1 << 31, n, dtype=np.int64).astype(np.int32)
+        assert np.array_equal(oracle.apse(a), oracle.ref_apse(a))
+        assert np.array_equal(oracle.apse(a, True), oracle.ref_apse(a, True))
+        d = rng.integers(0, 4, n).astype(np.int32)
+        assert np.array_equal(oracle.apse(d, False), oracle.ref_apse(d, False))
+        assert np.array_equal(oracle.apse(d, True), oracle.ref_apse(d, True))
