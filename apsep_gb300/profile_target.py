@@ -1,0 +1,58 @@
+"""Minimal profiling target (the role of the reference's src/profile_bottleneck.cu).
+
+    python -m apsep_gb300.profile_target [--dist uniform|descending|ascending|dup16]
+                                         [--n 33554432] [--reps 3] [--config 0] [--dtype int32|float32]
+
+Allocates one input and one output (2 * 4 * n bytes), runs `reps` APSE
+launches with a synchronisation after each, prints the last launch's time.
+Small enough on the device for ncu captures; n = 2^25 keeps the 128 MiB
+input above the 126 MiB L2.
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+import torch
+
+from apsep_gb300 import Plan
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--dist", default="uniform", choices=("uniform", "descending", "ascending", "dup16"))
+    ap.add_argument("--n", type=int, default=1 << 25)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--config", type=int, default=0)
+    ap.add_argument("--dtype", default="int32", choices=("int32", "float32"))
+    a = ap.parse_args()
+    rng = np.random.default_rng(7)
+    n = a.n
+    if a.dist == "uniform":
+        h = rng.integers(0, 1 << 31, n, dtype=np.int64)
+    elif a.dist == "descending":
+        h = np.arange(n - 1, -1, -1, dtype=np.int64)
+    elif a.dist == "ascending":
+        h = np.arange(n, dtype=np.int64)
+    else:
+        h = rng.integers(0, 16, n)
+    dt = torch.int32 if a.dtype == "int32" else torch.float32
+    x = torch.from_numpy(h.astype(np.int32 if a.dtype == "int32" else np.float32)).cuda()
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    plan = Plan(n, dt)
+    plan.set_config(a.config)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms = 0.0
+    for _ in range(a.reps):
+        e0.record()
+        plan.run(x, out=out)
+        e1.record()
+        plan.check()
+        ms = e0.elapsed_time(e1)
+    print("done dist=%s n=%d config=%d last=%.1f us (%.1f GB/s useful)" % (a.dist, n, a.config, ms * 1e3,
+                                                                         8.0 * n / (ms * 1e-3) / 1e9))
+    plan.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,341 @@
+"""Benchmark: single-array APSE at N = 2^25 int32 keys on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload ("apse_single_2p25_int32"): one step is one APSE pass over one
+2^25-key int32 array; the steps rotate over the four seeded distributions of
+the N=2^25 configuration -- uniform in [0, 2^31), strictly descending,
+strictly ascending, uniform in [0, 16) -- so every distribution is timed.
+Metric: useful GB/s = 2 * N * 4 B / time (read the keys, write the answers),
+aggregated over the timed steps; the per-distribution figures are reported
+beside it.
+
+  value      device time: CUDA events on the launching stream around each
+             apsep_run, inputs resident in HBM; L2 is flushed (512 MiB write)
+             before every step, outside the events.
+  e2e        the same metric through the public API with host buffers: each
+             step copies the keys from pinned host memory, runs, and copies
+             the answers back, all inside the timed events.
+  roofline   achieved = algorithmic bytes per launch (8 B/key) / mean launch
+             time, against the measured HBM copy bandwidth
+             (MEASURED_PEAKS.json); traffic = DRAM bytes per launch from the
+             committed ncu summary (profiles/), when present.
+  cpu_baseline  the sequential monotone-stack oracle on one host core over a
+             bounded sample (every distribution, full size).
+
+Multi-GPU (torchrun, one rank per GPU): the path does not shard, so every
+rank runs independent replicas of the same workload ("weak" scaling); value
+is all ranks' useful bytes over the slowest rank's time.
+
+--impl reference times the reference's sequential CPU algorithm (the oracle
+port of cpuApsep, src/main.cu:102-113) on the host cores, all threads busy on
+independent arrays, same workload, metric and units.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N = 1 << 25
+DISTS = ("uniform", "descending", "ascending", "dup16")
+METRIC = "useful GB/s at N=32M (frac. of HBM peak)"
+UNIT = "GB/s"
+WORKLOAD = "apse_single_2p25_int32"
+
+
+def make_inputs(n: int = N, seed: int = 20250325) -> dict[str, np.ndarray]:
+    rng = np.random.default_rng(seed)
+    return {
+        "uniform": rng.integers(0, 1 << 31, n, dtype=np.int64).astype(np.int32),
+        "descending": np.arange(n - 1, -1, -1, dtype=np.int32),
+        "ascending": np.arange(n, dtype=np.int32),
+        "dup16": rng.integers(0, 16, n).astype(np.int32),
+    }
+
+
+def useful_gbs(n: int, seconds: float, count: int = 1) -> float:
+    return 2.0 * n * 4 * count / seconds / 1e9
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic() -> dict | None:
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.isfile(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples: list[tuple[float, list[str]]] = []
+        self.proc = None
+        self.t = None
+        self.window = (0.0, 0.0)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def mark(self, t0, t1):
+        self.window = (t0, t1)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.12)
+        self.proc.terminate()
+        try:
+            self.proc.wait(2)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        t0, t1 = self.window
+        inside = [s for ts, s in self.samples if t0 - 0.05 <= ts <= t1 + 0.05]
+        used = inside if inside else [s for _, s in self.samples]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(s[1]) for s in used if len(s) >= 9 and num(s[1]) is not None]
+        mx = [num(s[2]) for s in used if len(s) >= 9 and num(s[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in used if len(s) >= 9 for i in range(4) if s[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(used), "window": "timed" if inside else "whole run"}
+
+
+def cpu_baseline(inputs: dict[str, np.ndarray], reps: int = 2) -> dict:
+    """The sequential oracle on one core: every distribution, full size."""
+    import oracle
+    oracle.build()
+    times = []
+    for _ in range(reps):
+        for name in DISTS:
+            t0 = time.perf_counter()
+            oracle.apse(inputs[name])
+            times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    return {"value": round(useful_gbs(N, tot, len(times)), 3), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d passes: %d reps x {%s} at N=2^25 int32, one thread, %.1f s" %
+                      (len(times), reps, ",".join(DISTS), tot)}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import concurrent.futures as cf
+
+    import oracle
+    oracle.build()
+    inputs = make_inputs()
+    threads = os.cpu_count() or 1
+    for i in range(args.warmup):
+        oracle.apse(inputs[DISTS[i % 4]])
+    order = [DISTS[i % 4] for i in range(args.steps)]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:  # ctypes releases the GIL
+        list(ex.map(lambda d: oracle.apse(inputs[d]), order))
+    wall = time.perf_counter() - t0
+    value = useful_gbs(N, wall, args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall * 1e3 / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "i32",
+        "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": WORKLOAD, "n": N, "distributions": list(DISTS), "cmp": "<"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d full-size passes on %d threads (independent arrays), sequential "
+                                   "monotone stack restating cpuApsep" % (args.steps, threads)},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from apsep_gb300 import Plan
+
+    dev = torch.device("cuda", local)
+    host = make_inputs(seed=20250325 + rank)
+    d_in = {k: torch.from_numpy(v).to(dev) for k, v in host.items()}
+    pinned_in = {k: torch.from_numpy(v).pin_memory() for k, v in host.items()}
+    pinned_out = torch.empty(N, dtype=torch.int32).pin_memory()
+    out = torch.empty(N, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    plan = Plan(N, torch.int32, device=dev)
+
+    def sanity(name):  # closed forms; no oracle on this path
+        o = out
+        if name == "ascending":
+            assert bool((o[1:] == torch.arange(0, N - 1, device=dev, dtype=torch.int32)).all()) and int(o[0]) == -1
+        elif name == "descending":
+            assert bool((o == -1).all())
+
+    for i in range(max(args.warmup, 3)):
+        name = DISTS[i % 4]
+        plan.run(d_in[name], out=out)
+        plan.check()
+        sanity(name)
+
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+        time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        plan.run(d_in[DISTS[i % 4]], out=out)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    if dist:
+        dist.barrier()
+    plan.check()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+
+    # e2e through the public API: pinned host -> device, run, device -> host
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    x_dev = torch.empty(N, dtype=torch.int32, device=dev)
+    for i in range(args.steps):
+        flush.zero_()
+        ev2[i][0].record(stream)
+        x_dev.copy_(pinned_in[DISTS[i % 4]], non_blocking=True)
+        plan.run(x_dev, out=out)
+        pinned_out.copy_(out, non_blocking=True)
+        ev2[i][1].record(stream)
+    torch.cuda.synchronize()
+    plan.check()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in ev2)
+
+    t = torch.tensor([total_ms, e2e_ms], dtype=torch.float64, device=dev)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms, e2e_ms = float(t[0]), float(t[1])
+    clocks = {}
+    if rank == 0:
+        sampler.mark(t_wall0, t_wall1)
+        clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    value = useful_gbs(N, total_ms / 1e3, args.steps * world)
+    per = {}
+    for j, name in enumerate(DISTS):
+        ms = [step_ms[i] for i in range(args.steps) if i % 4 == j]
+        if ms:
+            per[name] = {"gbs": round(useful_gbs(N, statistics.median(ms) / 1e3), 1),
+                         "us_median": round(statistics.median(ms) * 1e3, 2)}
+    peaks = measured_peaks()
+    mean_s = total_ms / 1e3 / args.steps
+    achieved = 8.0 * N / mean_s / 1e9
+    traffic = profile_traffic()
+    for name in per:
+        per[name]["frac"] = round(per[name]["gbs"] / peaks["hbm_gbs"], 4)
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "i32", "data": "synthetic (seeded numpy PCG64)",
+        "config": {"workload": WORKLOAD, "n": N, "distributions": list(DISTS), "cmp": "<",
+                   "l2": "flushed before every step (512 MiB write, outside the timed events)",
+                   "parallelism": "replicas x%d" % world},
+        "per_distribution": per,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": 8 * N,
+                     "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                     "traffic_source": traffic.get("source") if traffic else None},
+        "e2e": {"value": round(useful_gbs(N, e2e_ms / 1e3, args.steps * world), 2), "unit": UNIT,
+                "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "wall_s_timed_region": round(t_wall1 - t_wall0, 4),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(host)
+    print(json.dumps(line), flush=True)
+    plan.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()
