@@ -29,7 +29,10 @@ SIGNATURES = {
     "apsep_config_shape": ([_i32, ctypes.POINTER(_i32), ctypes.POINTER(_i32)], ctypes.c_int),
     "apsep_launch": ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "apsep_debug_inject": ([_vp, _i32, _u32], ctypes.c_int),
+    "apsep_run_noalloc": ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
 }
+
+NOALLOC_MAX_KEYS = 4194304  # APSEP_NOALLOC_MAX_KEYS in include/apsep.h
 
 APSEP_OK, APSEP_EINVAL, APSEP_ENOMEM, APSEP_ECUDA, APSEP_ETIMEOUT, APSEP_EINTERNAL, APSEP_ENOTSUP = range(7)
 INT32, FLOAT32 = 0, 1

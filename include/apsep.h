@@ -109,6 +109,24 @@ apsep_status apsep_config_shape(int32_t config, int32_t* threads, int32_t* keys_
  * (launchSPT / launchWSTL) */
 apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp);
 
+/* Largest n apsep_run_noalloc accepts (2^22 keys). */
+#define APSEP_NOALLOC_MAX_KEYS 4194304
+
+/* apsep_run without any device allocation, for callers that cannot allocate
+ * device memory at call time (a process that reserved the whole device heap
+ * for its own pool, or a path where cudaMalloc/cudaFree and their implicit
+ * synchronisation are not allowed).  No counterpart in the reference: its
+ * every entry point allocates or takes caller-allocated scratch.
+ * The scratch is a static device array sized for APSEP_NOALLOC_MAX_KEYS keys
+ * (about 540 KiB, held on every GPU that loads the library until exit);
+ * n > APSEP_NOALLOC_MAX_KEYS returns APSEP_EINVAL.  The first call on each
+ * device resolves the array's address and initialises it, so make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose kernels overlap on the GPU race, so serialise them (e.g. one
+ * stream).  Asynchronous on `stream`; device-side errors are not reported. */
+apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp,
+                               void* stream);
+
 /* Fault injection for failure-detection tests: the next run's tile `tile`
  * never publishes its look-back status, and every device wait gives up after
  * `spin_limit` polls, so its successors report APSEP_ETIMEOUT through

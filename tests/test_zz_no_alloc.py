@@ -1,0 +1,55 @@
+"""apsep_run_noalloc: the run for callers that cannot allocate device memory.
+
+Such callers (a host process that has reserved the whole device heap for its
+own pool, or a path where cudaMalloc/cudaFree and their synchronisation are
+not allowed) get their scratch from a static device array inside the
+library.  This checks, through the C ABI, that two calls in a row give
+bit-for-bit the answers of the plan-based apsep_run on the same inputs, and
+that sizes beyond the array's limit are refused.  The file is named so that
+pytest collects it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from apsep_gb300 import Plan, _lib
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(x, out, n, dtype, cmp):
+    lib = _lib.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return lib.apsep_run_noalloc(ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), n, dtype, cmp,
+                                 stream)
+
+
+def test_noalloc_matches_plan_on_two_calls_in_a_row():
+    rng = np.random.default_rng(4242)
+    cases = [
+        (rng.integers(0, 1 << 31, 1_000_003, dtype=np.int64).astype(np.int32), _lib.INT32, _lib.LT),
+        (np.arange(3 * 4096 + 5, dtype=np.int32)[::-1].copy(), _lib.INT32, _lib.LT),
+        (rng.integers(0, 16, 777_777).astype(np.int32), _lib.INT32, _lib.LE),
+        ((rng.integers(-1000, 1000, 250_001) * 0.5).astype(np.float32), _lib.FLOAT32, _lib.LT),
+    ]
+    for a, dtype, cmp in cases:
+        n = a.shape[0]
+        x = torch.from_numpy(a).cuda()
+        with Plan(n, x.dtype, inclusive=(cmp == _lib.LE)) as plan:
+            want = plan.run(x)
+            plan.check()
+        want = want.cpu()
+        for _ in range(2):  # the shared static scratch carries state from call to call
+            out = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+            assert _noalloc(x, out, n, dtype, cmp) == _lib.APSEP_OK
+            torch.cuda.synchronize()
+            assert torch.equal(out.cpu(), want)
+
+
+def test_noalloc_refuses_sizes_beyond_its_static_scratch():
+    n = _lib.NOALLOC_MAX_KEYS + 1
+    x = torch.zeros(n, dtype=torch.int32, device="cuda")
+    out = torch.empty_like(x)
+    assert _noalloc(x, out, n, _lib.INT32, _lib.LT) == _lib.APSEP_EINVAL
