@@ -86,8 +86,9 @@ class Plan:
         _lib.check(self._lib.apsep_plan_check(self._h, ctypes.c_void_p(_stream_handle(self.device, stream))),
                    "apsep_plan_check")
 
-    def debug_inject(self, tile: int, spin_limit: int) -> None:
-        _lib.check(self._lib.apsep_debug_inject(self._h, int(tile), int(spin_limit)), "apsep_debug_inject")
+    def debug_inject(self, range_index: int, spin_limit: int) -> None:
+        """Fault injection: in the next run, range `range_index` never publishes."""
+        _lib.check(self._lib.apsep_debug_inject(self._h, int(range_index), int(spin_limit)), "apsep_debug_inject")
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -22,15 +22,14 @@ struct apsep_plan {
     int64_t capacity = 0;
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
-    TileScratch ts{};
-    int dbg_skip_tile = -1;
+    RangeScratch rs{};
+    int dbg_skip_range = -1;
     uint32_t dbg_spin_limit = 0;
 };
 
 namespace {
 
 constexpr uint32_t kDefaultSpinLimit = 1u << 22;  // ~1 s of polling with back-off
-constexpr int kMinTileKeys = 2048;               // smallest tile of kTileConfigs
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
@@ -130,37 +129,26 @@ apsep_status apsep_plan_create(apsep_plan** out, apsep_dtype dtype, apsep_cmp cm
     p->dtype = dtype;
     p->cmp = cmp;
     p->capacity = capacity;
-    const int64_t cap = capacity > 0 ? capacity : 1;
-    const int64_t cap_tiles = (cap + kMinTileKeys - 1) / kMinTileKeys + 1;
-    const size_t off_state = align_up(sizeof(Counters), 256);
-    const size_t off_tmin = align_up(off_state + (size_t)cap_tiles * 8, 256);
-    const size_t off_cmin = align_up(off_tmin + (size_t)cap_tiles * 4, 256);
-    // chunk mins: num_tiles * tile/32 <= cap/32 + tile/32 for every tile size <= 8192
-    const size_t cmin_entries = (size_t)(cap + 31) / 32 + 8192 / 32;
-    const size_t total = align_up(off_cmin + cmin_entries * 4, 256);
+    const size_t total = carve_scratch(nullptr, capacity, nullptr);
     if (cudaMalloc(&p->scratch, total) != cudaSuccess) {
         cudaGetLastError();
         delete p;
         return APSEP_ENOMEM;
     }
     p->scratch_bytes = total;
-    char* base = (char*)p->scratch;
-    p->ts.ctr = (Counters*)base;
-    p->ts.state = (uint64_t*)(base + off_state);
-    p->ts.tile_min = base + off_tmin;
-    p->ts.chunk_min = base + off_cmin;
-    p->ts.cap_tiles = (int)cap_tiles;
+    carve_scratch(p->scratch, capacity, &p->rs);
     Counters c0;
     memset(&c0, 0, sizeof(c0));
     c0.epoch = 1;
     if (cudaMemset(p->scratch, 0, total) != cudaSuccess ||
-        cudaMemcpy(p->ts.ctr, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpy(p->rs.ctr, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(p->scratch);
         delete p;
         return APSEP_ECUDA;
     }
     for (int cfg = 0; cfg < kNumTileConfigs; cfg++)
-        if (single_prepare(cfg) != cudaSuccess) {
+        if (range_prepare(cfg) != cudaSuccess) {
+            cudaGetLastError();
             cudaFree(p->scratch);
             delete p;
             return APSEP_ECUDA;
@@ -219,18 +207,20 @@ apsep_status apsep_run_cmp(apsep_plan* p, const void* d_in, int32_t* d_out, int6
         if (!encode_rows(&mi, d_in, rows, tile_rows, p->dtype) || !encode_rows(&mo, d_out, rows, tile_rows, 0))
             return APSEP_ECUDA;
     }
-    SingleArgs a;
+    RangeArgs a;
     a.d_in = d_in;
     a.d_out = d_out;
     a.n = (int)n;
     a.num_tiles = (int)num_tiles;
+    a.tiles_per_range = 0;
+    a.num_ranges = 0;
     a.tma_rows = rows;
     a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
-    a.skip_publish_tile = p->dbg_skip_tile;
-    a.s = p->ts;
-    p->dbg_skip_tile = -1;  // one-shot
+    a.skip_publish_range = p->dbg_skip_range;
+    a.s = p->rs;
+    p->dbg_skip_range = -1;  // one-shot
     p->dbg_spin_limit = 0;
-    cudaError_t e = launch_single(p->dtype, cmp == APSEP_LE ? 1 : 0, p->cfg, a, mi, mo, (cudaStream_t)stream);
+    cudaError_t e = launch_range(p->dtype, cmp == APSEP_LE ? 1 : 0, p->cfg, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }
 
@@ -244,10 +234,10 @@ apsep_status apsep_plan_check(apsep_plan* p, void* stream) {
     DeviceGuard g(p->device);
     if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return APSEP_ECUDA;
     uint32_t err = 0;
-    if (cudaMemcpy(&err, &p->ts.ctr->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return APSEP_ECUDA;
+    if (cudaMemcpy(&err, &p->rs.ctr->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return APSEP_ECUDA;
     if (!err) return APSEP_OK;
     uint32_t zero = 0;
-    if (cudaMemcpy(&p->ts.ctr->err, &zero, 4, cudaMemcpyHostToDevice) != cudaSuccess) return APSEP_ECUDA;
+    if (cudaMemcpy(&p->rs.ctr->err, &zero, 4, cudaMemcpyHostToDevice) != cudaSuccess) return APSEP_ECUDA;
     if (err & (ERR_LOOKBACK_TIMEOUT | ERR_TMA_TIMEOUT)) return APSEP_ETIMEOUT;
     return APSEP_EINTERNAL;
 }
@@ -263,9 +253,9 @@ apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dty
     return s != APSEP_OK ? s : c;
 }
 
-apsep_status apsep_debug_inject(apsep_plan* p, int32_t tile, uint32_t spin_limit) {
-    if (!p || tile < -1) return APSEP_EINVAL;
-    p->dbg_skip_tile = tile;
+apsep_status apsep_debug_inject(apsep_plan* p, int32_t range, uint32_t spin_limit) {
+    if (!p || range < -1) return APSEP_EINVAL;
+    p->dbg_skip_range = range;
     p->dbg_spin_limit = spin_limit;
     return APSEP_OK;
 }

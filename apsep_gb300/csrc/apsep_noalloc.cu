@@ -8,7 +8,7 @@
 // the scratch this engine needs (control block, look-back words, tile and
 // chunk minima) lives in one file-scope __device__ array below, sized for at
 // most APSEP_NOALLOC_MAX_KEYS keys.  Every GPU that loads this library holds
-// that array (about 540 KiB) until the process exits.
+// that array (1,091,584 bytes) until the process exits.
 //
 // Host code must not pass the array's name to a kernel: on the host it is
 // only a stand-in symbol.  The first call on each device looks up the
@@ -29,12 +29,7 @@ using namespace apsep;
 namespace {
 
 constexpr int64_t kMaxKeys = APSEP_NOALLOC_MAX_KEYS;
-constexpr int64_t kTiles = kMaxKeys / 2048 + 2;  // smallest tile of any configuration
-constexpr size_t kOffState = 256;
-constexpr size_t kOffTileMin = (kOffState + (size_t)kTiles * 8 + 255) / 256 * 256;
-constexpr size_t kOffChunkMin = (kOffTileMin + (size_t)kTiles * 4 + 255) / 256 * 256;
-constexpr size_t kBytes = (kOffChunkMin + ((size_t)kMaxKeys / 32 + 256) * 4 + 255) / 256 * 256;
-static_assert(sizeof(Counters) <= kOffState, "control block must fit before the status words");
+constexpr size_t kBytes = scratch_offsets(kMaxKeys).total;  // the same layout a plan uses
 
 constexpr int kConfig = 0;                 // 256 threads x 16 keys per tile
 constexpr uint32_t kSpinLimit = 1u << 22;  // bound on every device-side wait
@@ -90,7 +85,7 @@ apsep_status scratch_for_current_device(void** out) {
         memset(&c0, 0, sizeof(c0));
         c0.epoch = 1;
         if (cudaMemcpy(p, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) return APSEP_ECUDA;
-        if (single_prepare(kConfig) != cudaSuccess) return APSEP_ECUDA;
+        if (range_prepare(kConfig) != cudaSuccess) return APSEP_ECUDA;
         g_addr[dev] = p;
     }
     *out = g_addr[dev];
@@ -113,15 +108,11 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
     apsep_status st = scratch_for_current_device(&base);
     if (st != APSEP_OK) return st;
 
-    TileScratch ts;
-    ts.ctr = (Counters*)base;
-    ts.state = (uint64_t*)((char*)base + kOffState);
-    ts.tile_min = (char*)base + kOffTileMin;
-    ts.chunk_min = (char*)base + kOffChunkMin;
-    ts.cap_tiles = (int)kTiles;
-    // The tile counters must start at zero; a completed run leaves them so,
+    RangeScratch rs;
+    carve_scratch(base, kMaxKeys, &rs);
+    // The range counters must start at zero; a completed run leaves them so,
     // this also covers a run that never completed.
-    if (cudaMemsetAsync(ts.ctr, 0, 2 * sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess) return APSEP_ECUDA;
+    if (cudaMemsetAsync(rs.ctr, 0, 2 * sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess) return APSEP_ECUDA;
 
     const TileConfig tc = kTileConfigs[kConfig];
     const int B = tc.nt * tc.ipt;
@@ -134,15 +125,17 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
     if (rows > 0 && (!encode(&mi, d_in, rows, tile_rows, dtype) || !encode(&mo, d_out, rows, tile_rows, 0)))
         return APSEP_ECUDA;
 
-    SingleArgs a;
+    RangeArgs a;
     a.d_in = d_in;
     a.d_out = d_out;
     a.n = (int)n;
     a.num_tiles = (int)((n + B - 1) / B);
+    a.tiles_per_range = 0;
+    a.num_ranges = 0;
     a.tma_rows = rows;
     a.spin_limit = kSpinLimit;
-    a.skip_publish_tile = -1;
-    a.s = ts;
-    cudaError_t e = launch_single(dtype, cmp == APSEP_LE ? 1 : 0, kConfig, a, mi, mo, (cudaStream_t)stream);
+    a.skip_publish_range = -1;
+    a.s = rs;
+    cudaError_t e = launch_range(dtype, cmp == APSEP_LE ? 1 : 0, kConfig, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }

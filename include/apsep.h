@@ -118,7 +118,7 @@ apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dty
  * synchronisation are not allowed).  No counterpart in the reference: its
  * every entry point allocates or takes caller-allocated scratch.
  * The scratch is a static device array sized for APSEP_NOALLOC_MAX_KEYS keys
- * (about 540 KiB, held on every GPU that loads the library until exit);
+ * (1,091,584 bytes, held on every GPU that loads the library until exit);
  * n > APSEP_NOALLOC_MAX_KEYS returns APSEP_EINVAL.  The first call on each
  * device resolves the array's address and initialises it, so make that
  * first call before any stream capture.  All calls share the array: calls
@@ -127,12 +127,13 @@ apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dty
 apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp,
                                void* stream);
 
-/* Fault injection for failure-detection tests: the next run's tile `tile`
- * never publishes its look-back status, and every device wait gives up after
- * `spin_limit` polls, so its successors report APSEP_ETIMEOUT through
- * apsep_plan_check instead of hanging.  tile = -1 restores normal runs
- * (spin_limit 0 = default). */
-apsep_status apsep_debug_inject(apsep_plan* plan, int32_t tile, uint32_t spin_limit);
+/* Fault injection for failure-detection tests: in the next run, range `range`
+ * (the contiguous block of tiles one persistent CTA sweeps) never publishes
+ * its look-back status, and every device wait gives up after `spin_limit`
+ * polls, so its successors report APSEP_ETIMEOUT through apsep_plan_check
+ * instead of hanging.  range = -1 restores normal runs (spin_limit 0 =
+ * default). */
+apsep_status apsep_debug_inject(apsep_plan* plan, int32_t range, uint32_t spin_limit);
 
 #ifdef __cplusplus
 }

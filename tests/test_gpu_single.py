@@ -126,7 +126,7 @@ def test_edge_sizes_vs_oracle(plans, name, le):
                                                                                want[bad]))
 
 
-@pytest.mark.parametrize("config", [0, 1, 2])
+@pytest.mark.parametrize("config", [0, 1])
 def test_every_config(config):
     rng = np.random.default_rng(77 + config)
     with Plan(300000, torch.int32) as plan:
@@ -212,15 +212,15 @@ def test_cuda_graph_capture(plans):
 
 
 def test_lookback_timeout_is_reported_not_hung():
-    """A predecessor tile that never publishes: the successors' bounded waits
-    give up, the run finishes, the host reads APSEP_ETIMEOUT, and the next
-    run on the same plan is correct again."""
+    """A predecessor range that never publishes: the successors' bounded
+    waits give up, the run finishes, the host reads APSEP_ETIMEOUT, and the
+    next run on the same plan is correct again.  (6 tiles -> 6 one-tile ranges.)"""
     n = 4096 * 6
     a = dist("uniform", n, np.random.default_rng(8))
     with Plan(n, torch.int32) as plan:
         x = torch.from_numpy(a).cuda()
         out = torch.empty_like(x)
-        plan.debug_inject(tile=2, spin_limit=2000)
+        plan.debug_inject(range_index=2, spin_limit=2000)
         plan.run(x, out=out)
         with pytest.raises(ApsepError) as ei:
             plan.check()
