@@ -107,7 +107,7 @@ int32_t apsep_num_configs(void) { return kNumTileConfigs; }
 
 apsep_status apsep_config_shape(int32_t config, int32_t* threads, int32_t* keys_per_thread) {
     if (config < 0 || config >= kNumTileConfigs) return APSEP_EINVAL;
-    if (threads) *threads = kTileConfigs[config].nt;
+    if (threads) *threads = kTileConfigs[config].wpc * 32;
     if (keys_per_thread) *keys_per_thread = kTileConfigs[config].ipt;
     return APSEP_OK;
 }
@@ -170,7 +170,7 @@ apsep_status apsep_plan_get_info(const apsep_plan* p, apsep_plan_info* info) {
     memset(info, 0, sizeof(*info));
     info->capacity = p->capacity;
     info->scratch_bytes = (int64_t)p->scratch_bytes;
-    info->tile_keys = kTileConfigs[p->cfg].nt * kTileConfigs[p->cfg].ipt;
+    info->tile_keys = 32 * kTileConfigs[p->cfg].ipt;  // one warp's tile
     info->config = p->cfg;
     info->device = p->device;
     info->dtype = p->dtype;
@@ -194,7 +194,7 @@ apsep_status apsep_run_cmp(apsep_plan* p, const void* d_in, int32_t* d_out, int6
     if (!g.ok) return APSEP_ECUDA;
 
     const TileConfig tc = kTileConfigs[p->cfg];
-    const int B = tc.nt * tc.ipt;
+    const int B = 32 * tc.ipt;  // keys per warp tile
     const int tile_rows = B / 32;
     const int64_t num_tiles = (n + B - 1) / B;
     int rows = (int)(n / 32);
@@ -236,8 +236,16 @@ apsep_status apsep_plan_check(apsep_plan* p, void* stream) {
     uint32_t err = 0;
     if (cudaMemcpy(&err, &p->rs.ctr->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return APSEP_ECUDA;
     if (!err) return APSEP_OK;
-    uint32_t zero = 0;
-    if (cudaMemcpy(&p->rs.ctr->err, &zero, 4, cudaMemcpyHostToDevice) != cudaSuccess) return APSEP_ECUDA;
+    // A run that gave up may have left counters half-way: re-arm the control
+    // region (counters, group counters) keeping the epoch.
+    Counters c0;
+    if (cudaMemcpy(&c0, p->rs.ctr, sizeof(c0), cudaMemcpyDeviceToHost) != cudaSuccess) return APSEP_ECUDA;
+    const uint32_t epoch = c0.epoch;
+    memset(&c0, 0, sizeof(c0));
+    c0.epoch = epoch;
+    if (cudaMemset(p->scratch, 0, control_bytes()) != cudaSuccess ||
+        cudaMemcpy(p->rs.ctr, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess)
+        return APSEP_ECUDA;
     if (err & (ERR_LOOKBACK_TIMEOUT | ERR_TMA_TIMEOUT)) return APSEP_ETIMEOUT;
     return APSEP_EINTERNAL;
 }

@@ -23,18 +23,23 @@ constexpr uint32_t EPOCH_LIMIT = (1u << 30) - 1u;
 // CTA resets the counters and advances the epoch), so runs need no memset
 // and can be captured in a CUDA graph.
 struct alignas(64) Counters {
-    uint32_t range_counter;  // next dynamic range id
-    uint32_t done;           // CTAs finished in the current run
+    uint32_t range_counter;  // next dynamic range id (one range per warp)
+    uint32_t done;           // warps finished in the current run
     uint32_t epoch;          // tag of the current run's status words, 1..EPOCH_LIMIT
     uint32_t err;            // ERR_* bits, sticky until read
-    uint32_t pad[12];
+    uint32_t finished;       // groups of 32 ranges that published their minimum in the current run
+    uint32_t pad[11];
 };
 
 // Scratch of one run, carved from one device allocation (or the static
 // array of apsep_run_noalloc) by carve_scratch().
 struct RangeScratch {
     Counters* ctr;
-    uint64_t* range_state;  // [max_ranges] look-back words: tag<<32 | key bits
+    uint32_t* group_cnt;    // [max_ranges/32] ranges of each group of 32 done in this run
+    uint64_t* group_state;  // [max_ranges/32] tag<<32 | key bits: min of a finished group
+    uint32_t* group_pre;    // [max_ranges/32] key bits: min of the groups before (once cta_ready says so)
+    uint32_t* cta_ready;    // [kMaxCtas * kReadyStride] epoch whose group_pre is complete, one line per CTA
+    uint64_t* range_state;  // [max_ranges] tag<<32 | key bits: min of a finished range
     void* range_min;        // [max_ranges] key: min of each range
     void* tile_min;         // [cap_tiles]  key: min of each tile
     uint64_t* tile_rpre;    // [cap_tiles]  has<<32 | bits: min of the range's keys before the tile
@@ -45,13 +50,15 @@ struct RangeScratch {
     int max_ranges;
 };
 
-constexpr int kMinTileKeys = 4096;  // smallest tile of any configuration
-constexpr int kMaxTileKeys = 4096;  // largest tile of any configuration
-constexpr int kMaxRanges = 2048;    // persistent CTAs per run, upper bound
+constexpr int kMinTileKeys = 256;   // smallest tile of any configuration (one warp's)
+constexpr int kMaxTileKeys = 512;   // largest tile of any configuration
+constexpr int kMaxRanges = 4096;    // persistent warps per run, upper bound
+constexpr int kMaxCtas = kMaxRanges / 8;  // every configuration runs >= 8 warps per CTA
+constexpr int kReadyStride = 16;          // words between two CTAs' ready flags (64 bytes)
 
 // Byte offsets of the scratch arrays for `capacity` keys (256-byte aligned).
 struct ScratchOffsets {
-    size_t state, rmin, tmin, rpre, cmin, dcnt, dmask, total;
+    size_t gcnt, gstate, gpre, ready, state, rmin, tmin, rpre, cmin, dcnt, dmask, total;
     int64_t cap_tiles;
 };
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -60,7 +67,11 @@ constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
     const int64_t cap = capacity > 0 ? capacity : 1;
     o.cap_tiles = (cap + kMinTileKeys - 1) / kMinTileKeys + 1;
     const size_t cap_chunks = (size_t)(cap + 31) / 32 + kMaxTileKeys / 32;
-    o.state = align256(sizeof(Counters));
+    o.gcnt = align256(sizeof(Counters));  // the control region: Counters + group counters
+    o.gstate = align256(o.gcnt + (size_t)(kMaxRanges / 32) * 4);
+    o.gpre = align256(o.gstate + (size_t)(kMaxRanges / 32) * 8);
+    o.ready = align256(o.gpre + (size_t)(kMaxRanges / 32) * 4);
+    o.state = align256(o.ready + (size_t)kMaxCtas * kReadyStride * 4);
     o.rmin = align256(o.state + (size_t)kMaxRanges * 8);
     o.tmin = align256(o.rmin + (size_t)kMaxRanges * 4);
     o.rpre = align256(o.tmin + (size_t)o.cap_tiles * 4);
@@ -70,6 +81,10 @@ constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
     o.total = align256(o.dmask + (size_t)o.cap_tiles * (kMaxTileKeys / 32) * 4);
     return o;
 }
+
+// The control region (Counters + group counters) must start zeroed; a run
+// leaves it zeroed, a run that timed out may not (apsep_plan_check clears it).
+constexpr size_t control_bytes() { return align256(sizeof(Counters)) + (size_t)(kMaxRanges / 32) * 4; }
 
 // Bytes of scratch for `capacity` keys; when base != nullptr also fills *s.
 size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s);
@@ -87,9 +102,9 @@ struct RangeArgs {
     RangeScratch s;
 };
 
-// A kernel configuration: threads per CTA x keys per thread.
+// A kernel configuration: warps per CTA x keys per lane (a warp's tile is 32*ipt keys).
 struct TileConfig {
-    int nt;
+    int wpc;
     int ipt;
 };
 constexpr int kNumTileConfigs = 2;

@@ -8,7 +8,7 @@
 // the scratch this engine needs (control block, look-back words, tile and
 // chunk minima) lives in one file-scope __device__ array below, sized for at
 // most APSEP_NOALLOC_MAX_KEYS keys.  Every GPU that loads this library holds
-// that array (1,091,584 bytes) until the process exits.
+// that array (1,920,512 bytes) until the process exits.
 //
 // Host code must not pass the array's name to a kernel: on the host it is
 // only a stand-in symbol.  The first call on each device looks up the
@@ -31,7 +31,7 @@ namespace {
 constexpr int64_t kMaxKeys = APSEP_NOALLOC_MAX_KEYS;
 constexpr size_t kBytes = scratch_offsets(kMaxKeys).total;  // the same layout a plan uses
 
-constexpr int kConfig = 0;                 // 256 threads x 16 keys per tile
+constexpr int kConfig = 0;                 // 8 warps per CTA, 512-key warp tiles
 constexpr uint32_t kSpinLimit = 1u << 22;  // bound on every device-side wait
 constexpr int kMaxDevices = 64;
 
@@ -110,12 +110,15 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
 
     RangeScratch rs;
     carve_scratch(base, kMaxKeys, &rs);
-    // The range counters must start at zero; a completed run leaves them so,
-    // this also covers a run that never completed.
-    if (cudaMemsetAsync(rs.ctr, 0, 2 * sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess) return APSEP_ECUDA;
+    // The range and group counters must start at zero; a completed run leaves
+    // them so, this also covers a run that never completed.
+    if (cudaMemsetAsync(rs.ctr, 0, 2 * sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess ||
+        cudaMemsetAsync(&rs.ctr->finished, 0, sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess ||
+        cudaMemsetAsync(rs.group_cnt, 0, (size_t)(kMaxRanges / 32) * 4, (cudaStream_t)stream) != cudaSuccess)
+        return APSEP_ECUDA;
 
     const TileConfig tc = kTileConfigs[kConfig];
-    const int B = tc.nt * tc.ipt;
+    const int B = 32 * tc.ipt;  // keys per warp tile
     const int tile_rows = B / 32;
     int rows = (int)(n / 32);
     CUtensorMap mi, mo;
