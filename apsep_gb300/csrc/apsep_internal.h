@@ -40,12 +40,13 @@ struct RangeScratch {
     uint32_t* group_pre;    // [max_ranges/32] key bits: min of the groups before (once cta_ready says so)
     uint32_t* cta_ready;    // [kMaxCtas * kReadyStride] epoch whose group_pre is complete, one line per CTA
     uint64_t* range_state;  // [max_ranges] tag<<32 | key bits: min of a finished range
-    void* range_min;        // [max_ranges] key: min of each range
+    void* top_key;          // [max_ranges * kTopEntries] key: top of each range's final stack, bottom first
+    int32_t* top_pos;       // [max_ranges * kTopEntries] their positions
+    uint32_t* top_cnt;      // [max_ranges] entries published | bit 31: they are the whole stack
     void* tile_min;         // [cap_tiles]  key: min of each tile
-    uint64_t* tile_rpre;    // [cap_tiles]  has<<32 | bits: min of the range's keys before the tile
     void* chunk_min;        // [cap_chunks] key: min of each 32-key chunk
-    int32_t* tile_defcnt;   // [cap_tiles]  keys of the tile left for the range's second phase
-    uint32_t* tile_defmask; // [cap_tiles * kMaxTileKeys/32] which keys (when 0 < count < tile)
+    uint32_t* tile_flag;    // [cap_tiles]  flagged keys of the tile | bit 31: some are capped
+    uint32_t* tile_mask;    // [cap_tiles * kMaxTileKeys/32] which keys are flagged
     int cap_tiles;
     int max_ranges;
 };
@@ -55,10 +56,11 @@ constexpr int kMaxTileKeys = 512;   // largest tile of any configuration
 constexpr int kMaxRanges = 4096;    // persistent warps per run, upper bound
 constexpr int kMaxCtas = kMaxRanges / 8;  // every configuration runs >= 8 warps per CTA
 constexpr int kReadyStride = 16;          // words between two CTAs' ready flags (64 bytes)
+constexpr int kTopEntries = 32;           // stack entries each range publishes for later ranges
 
 // Byte offsets of the scratch arrays for `capacity` keys (256-byte aligned).
 struct ScratchOffsets {
-    size_t gcnt, gstate, gpre, ready, state, rmin, tmin, rpre, cmin, dcnt, dmask, total;
+    size_t gcnt, gstate, gpre, ready, state, topk, topp, topc, tmin, cmin, flag, mask, total;
     int64_t cap_tiles;
 };
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -72,13 +74,14 @@ constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
     o.gpre = align256(o.gstate + (size_t)(kMaxRanges / 32) * 8);
     o.ready = align256(o.gpre + (size_t)(kMaxRanges / 32) * 4);
     o.state = align256(o.ready + (size_t)kMaxCtas * kReadyStride * 4);
-    o.rmin = align256(o.state + (size_t)kMaxRanges * 8);
-    o.tmin = align256(o.rmin + (size_t)kMaxRanges * 4);
-    o.rpre = align256(o.tmin + (size_t)o.cap_tiles * 4);
-    o.cmin = align256(o.rpre + (size_t)o.cap_tiles * 8);
-    o.dcnt = align256(o.cmin + cap_chunks * 4);
-    o.dmask = align256(o.dcnt + (size_t)o.cap_tiles * 4);
-    o.total = align256(o.dmask + (size_t)o.cap_tiles * (kMaxTileKeys / 32) * 4);
+    o.topk = align256(o.state + (size_t)kMaxRanges * 8);
+    o.topp = align256(o.topk + (size_t)kMaxRanges * kTopEntries * 4);
+    o.topc = align256(o.topp + (size_t)kMaxRanges * kTopEntries * 4);
+    o.tmin = align256(o.topc + (size_t)kMaxRanges * 4);
+    o.cmin = align256(o.tmin + (size_t)o.cap_tiles * 4);
+    o.flag = align256(o.cmin + cap_chunks * 4);
+    o.mask = align256(o.flag + (size_t)o.cap_tiles * 4);
+    o.total = align256(o.mask + (size_t)o.cap_tiles * (kMaxTileKeys / 32) * 4);
     return o;
 }
 

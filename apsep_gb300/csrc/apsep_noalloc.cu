@@ -8,7 +8,7 @@
 // the scratch this engine needs (control block, look-back words, tile and
 // chunk minima) lives in one file-scope __device__ array below, sized for at
 // most APSEP_NOALLOC_MAX_KEYS keys.  Every GPU that loads this library holds
-// that array (1,920,512 bytes) until the process exits.
+// that array (2,837,760 bytes) until the process exits.
 //
 // Host code must not pass the array's name to a kernel: on the host it is
 // only a stand-in symbol.  The first call on each device looks up the

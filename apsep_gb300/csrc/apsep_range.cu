@@ -2,47 +2,42 @@
 // warp-independent ranges.
 //
 // One launch.  Every WARP is an independent worker: it claims a contiguous
-// RANGE of warp tiles (32 lanes x IPT keys) from an atomic counter (so every
-// range it may wait on belongs to a warp that is already running), keeps its
-// own ring of TMA stages, its own answer-chain buffers and its own stack in
-// shared memory, and synchronises only with __syncwarp -- there is no
-// CTA-wide barrier anywhere.
+// RANGE of warp tiles (32 lanes x IPT keys) from an atomic counter, keeps its
+// own ring of TMA stages, its own answer buffers and its own stack in shared
+// memory, and synchronises only with __syncwarp -- there is no CTA-wide
+// barrier anywhere.
 //
 //  Phase 1, per warp tile (the next tiles' 128-byte-swizzled TMA loads stay
 //  in flight in the warp's ring):
-//   1. in-thread ANSV over IPT consecutive keys in registers (compare
+//   1. in-thread answers over IPT consecutive keys in registers (compare
 //      ladder) -- the in-thread step of apsepKernelSPT (src/apsep.cuh:2701-2707);
-//   2. warp prefix/suffix mins over lane mins (src/apsep.cuh:2709-2730) and
-//      the lane chain by warp-uniform pointer jumping (src/apsep.cuh:2734-2752);
-//   3. keys unresolved in-thread walk the tile's answer chain in shared
-//      memory: a key's next candidate is its in-thread answer, or, for a
-//      lane's minimum, the last key of its chain lane -- one pointer walk in
-//      place of the reference's spine walk + cross-warp fallback
-//      (src/apsep.cuh:2754-2801);
-//   4. keys with no answer in the tile query the warp's RANGE STACK: the
-//      strict suffix minima of the range's earlier tiles (binary search).
-//      This replaces the reference's global min-tree descent
-//      (src/apsep.cuh:2952-2996) for every answer inside the range;
-//   5. keys with no answer in the range are "deferred" (the range's prefix
-//      minima) -- only they wait for the global prefix;
-//   6. the tile's answers leave shared memory in one TMA store; the stack
-//      takes the tile's strict suffix minima.
-//  Then the warp publishes its range minimum as a decoupled look-back
-//  aggregate and looks back over earlier ranges (helping them publish their
-//  inclusive values) for the exclusive prefix minimum P.  Every wait is
-//  bounded and reports ERR_LOOKBACK_TIMEOUT / ERR_TMA_TIMEOUT.
+//   2. warp prefix minima over lane minima (src/apsep.cuh:2709-2730);
+//   3. each key without an in-thread answer is classified: answered by an
+//      earlier lane of the tile (X), by an earlier tile of the range (S), or by
+//      nothing in the range (deferred);
+//   4. X keys, spread evenly over the lanes, find their lane by binary lifting
+//      over a 5-level table of lane minima held in registers and their key by
+//      binary search over that lane's suffix minima -- a fixed number of
+//      steps in place of the reference's warp-uniform pointer jumping, spine
+//      walk and cross-warp fallback (src/apsep.cuh:2734-2801);
+//   5. S keys binary-search the warp's RANGE STACK (strict suffix minima of
+//      the range's earlier tiles), in place of the reference's global
+//      min-tree descent (src/apsep.cuh:2952-2996) for every answer inside the
+//      range;
+//   6. the whole tile leaves shared memory in one TMA store, deferred keys as
+//      -1; the stack takes the tile's strict suffix minima.
+//  Then the warp publishes its range minimum and the top of its stack, and
+//  reads the exclusive prefix minimum P of the earlier ranges (one handshake
+//  per launch, see range_publish).  Every wait is bounded and reports
+//  ERR_LOOKBACK_TIMEOUT / ERR_TMA_TIMEOUT.
 //
-//  Phase 2: the deferred keys are non-increasing, so those P qualifies form a
-//  prefix (pass A: in order, one monotone cursor, a warp-cooperative search
-//  through tile mins / chunk mins / one 32-key row); every later one answers
-//  -1 (pass B: straight from the deferred bitmask, whole tiles as one TMA
-//  store of -1) -- the reference's prefix-min early-out
-//  (src/apsep.cuh:2903-2926).
-//
-// Compared with the reference's three grid-wide phases there is no
-// grid.sync(); the only cross-warp waits are one look-back per range.  Every
-// output word is written once (phase 1 skips deferred keys, phase 2 writes
-// exactly those).
+//  Phase 2 touches only the flagged keys.  Deferred keys are the range's
+//  prefix minima, non-increasing, so the ones P qualifies form a prefix (the
+//  reference's prefix-min early-out, src/apsep.cuh:2903-2926); each finds
+//  the nearest earlier range whose minimum qualifies and its answer at the
+//  top of that range's published stack, all lanes in parallel.  Everything
+//  else (stacks that dropped entries, lists that overflowed) falls back to a
+//  warp-cooperative search down the min hierarchy (find_left).
 #include "apsep_device.cuh"
 #include "apsep_internal.h"
 
@@ -54,7 +49,9 @@ const TileConfig kTileConfigs[kNumTileConfigs] = {
 };
 
 constexpr int kStages = 3;      // TMA ring depth per warp (tiles)
-constexpr int kStackCap = 256;  // range-stack entries kept per warp
+constexpr int kStackCap = 128;  // range-stack entries kept per warp
+constexpr int kDefCap = 64;     // deferred keys listed in shared memory per range
+constexpr int kCapCap = 32;     // capped keys listed in shared memory per range
 
 // Shared memory of one warp.
 template <int IPT>
@@ -62,13 +59,18 @@ struct WLayout {
     static constexpr int WT = 32 * IPT;                              // keys per warp tile
     static constexpr size_t kV = 0;                                   // T[S][WT], swizzled (TMA dst)
     static constexpr size_t kO = kV + (size_t)kStages * WT * 4;       // int32[WT], swizzled (TMA src)
-    static constexpr size_t kNext = kO + (size_t)WT * 4;              // int16[WT]
-    static constexpr size_t kStkV = kNext + (size_t)WT * 2;           // T[K]
+    static constexpr size_t kSM = kO + (size_t)WT * 4;                // T[WT], swizzled: lane suffix minima
+    static constexpr size_t kList = kSM + (size_t)WT * 4;             // int16[WT]: X keys in order
+    static constexpr size_t kStkV = kList + (size_t)WT * 2;           // T[K]
     static constexpr size_t kStkP = kStkV + (size_t)kStackCap * 4;    // int32[K]
-    static constexpr size_t kBar = kStkP + (size_t)kStackCap * 4;     // uint64[S]
+    static constexpr size_t kDefP = kStkP + (size_t)kStackCap * 4;    // int32[kDefCap]
+    static constexpr size_t kDefV = kDefP + (size_t)kDefCap * 4;      // T[kDefCap]
+    static constexpr size_t kCapP = kDefV + (size_t)kDefCap * 4;      // int32[kCapCap]
+    static constexpr size_t kBar = (kCapP + (size_t)kCapCap * 4 + 7) / 8 * 8;  // uint64[S]
     static constexpr size_t kEnd = kBar + (size_t)kStages * 8;
     static constexpr size_t kBytes = (kEnd + 1023) / 1024 * 1024;     // keeps every warp 1024-aligned
-    static_assert(kO % 1024 == 0 && (WT * 4) % 1024 == 0, "swizzled buffers need 1024-byte alignment");
+    static_assert(kO % 1024 == 0 && kSM % 1024 == 0 && (WT * 4) % 1024 == 0,
+                  "swizzled buffers need 1024-byte alignment");
 };
 
 template <int IPT, int WPC>
@@ -100,6 +102,18 @@ __device__ __forceinline__ int ballot_last(int lo, int hi, T q, Load load) {
     const bool ok = i >= lo && lt<INCL>(load(i), q);
     const unsigned m = __ballot_sync(0xffffffffu, ok);
     return m ? hi - (__ffs(m) - 1) : -1;
+}
+
+// Exclusive prefix sum over the warp's lanes of a count c, and the total.
+__device__ __forceinline__ int warp_excl_sum(int c, int& total) {
+    int x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int nb = __shfl_up_sync(0xffffffffu, x, o);
+        if ((int)(threadIdx.x & 31) >= o) x += nb;
+    }
+    total = __shfl_sync(0xffffffffu, x, 31);
+    return x - c;
 }
 
 template <typename T, int B, bool INCL>
@@ -303,8 +317,9 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     constexpr int W = WT / 32;     // 32-key chunks (and TMA rows) per warp tile
     constexpr int TPC = 32 / IPT;  // lanes per chunk
     constexpr int K = kStackCap;
-    constexpr int MW = kMaxTileKeys / 32;  // deferred-mask words per tile in global
+    constexpr int MW = kMaxTileKeys / 32;  // flag-mask words per tile in global
     static_assert(IPT == 8 || IPT == 16, "IPT must be 8 or 16");
+    static_assert((K & (K - 1)) == 0, "the stack ring needs a power-of-two size");
     constexpr unsigned FULL = 0xffffffffu;
 
     extern __shared__ unsigned char smem_raw[];
@@ -314,9 +329,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023) + (size_t)warp * L::kBytes;
     T* sV = (T*)(wsm + L::kV);
     int32_t* O = (int32_t*)(wsm + L::kO);
-    int16_t* sNext = (int16_t*)(wsm + L::kNext);
+    T* sSM = (T*)(wsm + L::kSM);
+    int16_t* sList = (int16_t*)(wsm + L::kList);
     T* sStkV = (T*)(wsm + L::kStkV);
     int32_t* sStkP = (int32_t*)(wsm + L::kStkP);
+    int32_t* sDefP = (int32_t*)(wsm + L::kDefP);
+    T* sDefV = (T*)(wsm + L::kDefV);
+    int32_t* sCapP = (int32_t*)(wsm + L::kCapP);
     uint64_t* bar = (uint64_t*)(wsm + L::kBar);
 
     const T* d_in = (const T*)a.d_in;
@@ -349,10 +368,14 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     tma_load_2d(sV + (size_t)i * WT, &map_in, 0, (t0 + i) * W, &bar[i]);
                 }
         }
-        // Range stack state (warp-uniform).
-        int stk_top = 0, stk_lo = 0;
+        // Range state (warp-uniform): the stack ring [stk_lo, stk_hi) of strict
+        // suffix minima, values increasing from bottom to top; whether entries were
+        // ever dropped from its bottom; the range minimum so far; flagged-key counts.
+        int stk_lo = 0, stk_hi = 0;
+        bool dropped = false;
         bool has_rmin = false;
         T rmin = KeyTraits<T>::pad();
+        int def_total = 0, cap_total = 0;
 
         // ======================= phase 1: the range's tiles =======================
         for (int i = 0; i < ntr; i++) {
@@ -363,7 +386,6 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             const bool full = tile_full(t);
             const int tile_base = t * WT;
             const int valid_keys = min(WT, a.n - tile_base);
-            const bool last_of_range = (i == ntr - 1);
 
             if (full) {
                 if (!mbar_wait_bounded(&bar[slot], par, a.spin_limit) && lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
@@ -378,7 +400,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             if (lane == 0) bulk_wait_read0();  // the previous tile's store has read O
             __syncwarp();
 
-            // ---- 1. in-thread ANSV -----------------------------------------------------
+            // ---- 1. in-thread answers: compare ladder over IPT keys in registers --------
             T v[IPT];
 #pragma unroll
             for (int q4 = 0; q4 < IPT / 4; q4++) {
@@ -388,11 +410,15 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 v[4 * q4 + 2] = KeyTraits<T>::from_bits(rr.z);
                 v[4 * q4 + 3] = KeyTraits<T>::from_bits(rr.w);
             }
-            int res[IPT];
-            res[0] = -1;
+            const int lb = tile_base + lane * IPT;  // position of this lane's first key
+            const int nvalid = min(max(a.n - lb, 0), IPT);
+            unsigned umask = 0;     // keys without an in-thread answer
+            bool all_inc = false;   // the whole tile increases: every key answers its predecessor
             {
-                // If every lane's keys are monotone (each answers its neighbour, or
-                // none does), the in-thread answers follow without the ladder.
+                int res[IPT];  // absolute answers, -1 = none in the thread
+                res[0] = -1;
+                // Monotone lanes (each key answers its neighbour, or no key answers any
+                // later one) need no ladder.
                 bool adj = true, none = true;
 #pragma unroll
                 for (int k = 1; k < IPT; k++) {
@@ -402,172 +428,282 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 }
                 if (__all_sync(FULL, adj || none)) {
 #pragma unroll
-                    for (int k = 1; k < IPT; k++) res[k] = adj ? k - 1 : -1;
+                    for (int k = 1; k < IPT; k++) res[k] = adj ? lb + k - 1 : -1;
+                    // every key answers its predecessor across lane boundaries too
+                    const T prev_last = __shfl_up_sync(FULL, v[IPT - 1], 1);
+                    all_inc = __all_sync(FULL, adj && (lane == 0 || lt<INCL>(prev_last, v[0]))) && valid_keys == WT;
+                    if (all_inc && lane > 0) res[0] = lb - 1;
                 } else {
 #pragma unroll
                     for (int k = 1; k < IPT; k++) {
                         int rk = -1;
 #pragma unroll
                         for (int j = 0; j < k; j++)
-                            if (lt<INCL>(v[j], v[k])) rk = j;
+                            if (lt<INCL>(v[j], v[k])) rk = lb + j;
                         res[k] = rk;
                     }
                 }
+#pragma unroll
+                for (int k = 0; k < IPT; k++)
+                    if (res[k] < 0 && k < nvalid) umask |= 1u << k;
+                // in-thread answers; every other key holds -1 until resolved below
+#pragma unroll
+                for (int q4 = 0; q4 < IPT / 4; q4++)
+                    *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) =
+                        make_int4(res[4 * q4], res[4 * q4 + 1], res[4 * q4 + 2], res[4 * q4 + 3]);
             }
-            T tmin = v[0];
+            T lmin;
+            {  // suffix minima of the lane's keys (for the key search of X keys)
+                T sfx[IPT];
+                sfx[IPT - 1] = v[IPT - 1];
 #pragma unroll
-            for (int k = 1; k < IPT; k++) tmin = KeyTraits<T>::vmin(tmin, v[k]);
-            {
-                T cm = tmin;
+                for (int k = IPT - 2; k >= 0; k--) sfx[k] = KeyTraits<T>::vmin(v[k], sfx[k + 1]);
+                lmin = sfx[0];
 #pragma unroll
-                for (int o = 1; o < TPC; o <<= 1) cm = KeyTraits<T>::vmin(cm, __shfl_xor_sync(FULL, cm, o));
-                if ((lane & (TPC - 1)) == 0) __stcg(&chunk_min_w[(size_t)t * W + lane / TPC], cm);
+                for (int q4 = 0; q4 < IPT / 4; q4++)
+                    *reinterpret_cast<uint4*>(&sSM[swz(lane * IPT + 4 * q4)]) =
+                        make_uint4(KeyTraits<T>::bits(sfx[4 * q4]), KeyTraits<T>::bits(sfx[4 * q4 + 1]),
+                                   KeyTraits<T>::bits(sfx[4 * q4 + 2]), KeyTraits<T>::bits(sfx[4 * q4 + 3]));
             }
-            const int nvalid = min(max(a.n - (tile_base + lane * IPT), 0), IPT);
-            unsigned umask = 0;
-#pragma unroll
-            for (int k = 0; k < IPT; k++)
-                if (res[k] < 0 && k < nvalid) umask |= 1u << k;
             {
-                const int b = tile_base + lane * IPT;
+                T cmn = lmin;
 #pragma unroll
-                for (int q4 = 0; q4 < IPT / 4; q4++) {
-                    int4 o;
-                    o.x = res[4 * q4 + 0] >= 0 ? b + res[4 * q4 + 0] : -1;
-                    o.y = res[4 * q4 + 1] >= 0 ? b + res[4 * q4 + 1] : -1;
-                    o.z = res[4 * q4 + 2] >= 0 ? b + res[4 * q4 + 2] : -1;
-                    o.w = res[4 * q4 + 3] >= 0 ? b + res[4 * q4 + 3] : -1;
-                    *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) = o;
-                }
+                for (int o = 1; o < TPC; o <<= 1) cmn = KeyTraits<T>::vmin(cmn, __shfl_xor_sync(FULL, cmn, o));
+                if ((lane & (TPC - 1)) == 0) __stcg(&chunk_min_w[(size_t)t * W + lane / TPC], cmn);
             }
 
-            // ---- 2. warp prefix / suffix mins, lane chain, next-pointers ------------------
-            T pre = tmin;
+            // ---- 2. warp prefix minima over lane minima ---------------------------------
+            T pre = lmin;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const T nb = __shfl_up_sync(FULL, pre, o);
                 if (lane >= o) pre = KeyTraits<T>::vmin(pre, nb);
             }
-            const T carry = __shfl_up_sync(FULL, pre, 1);  // min of lanes < this one (lane > 0)
+            const T before = __shfl_up_sync(FULL, pre, 1);  // min of the lanes before (lane > 0)
             const T tile_min_t = __shfl_sync(FULL, pre, 31);
-            T suf = tmin;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const T nb = __shfl_down_sync(FULL, suf, o);
-                if (lane + o < 32) suf = KeyTraits<T>::vmin(suf, nb);
-            }
-            const T after_w = __shfl_down_sync(FULL, suf, 1);  // min of lanes > this one (lane < 31)
-            // Lane chain: the nearest earlier lane whose min qualifies for this lane's
-            // min (pointer jumping; invariant: every lane strictly between g and this
-            // lane fails lt(., tmin); g only decreases, <= 31 rounds).
-            int g = (lane > 0 && lt<INCL>(carry, tmin)) ? lane - 1 : -1;
-            for (int round = 0; round < 32; round++) {
-                const int src = g >= 0 ? g : lane;
-                const T tg = __shfl_sync(FULL, tmin, src);
-                const int gg = __shfl_sync(FULL, g, src);
-                const bool jump = g >= 0 && !lt<INCL>(tg, tmin);
-                if (!__any_sync(FULL, jump)) break;
-                if (jump) g = gg;
-            }
-            {
-                // Next candidate after a key that does not qualify for a query: its
-                // in-thread answer; for a key with none (the lane's minimum, which then
-                // bounds the whole lane) the last key of the chain lane.
-                const int jump = g >= 0 ? g * IPT + IPT - 1 : -1;
-                uint32_t pk[IPT / 2];
-#pragma unroll
-                for (int p = 0; p < IPT / 2; p++) {
-                    const int a0 = res[2 * p] >= 0 ? lane * IPT + res[2 * p] : jump;
-                    const int a1 = res[2 * p + 1] >= 0 ? lane * IPT + res[2 * p + 1] : jump;
-                    pk[p] = ((uint32_t)a0 & 0xffffu) | ((uint32_t)a1 << 16);
-                }
-                uint4* dst = reinterpret_cast<uint4*>(&sNext[lane * IPT]);
-                dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                if constexpr (IPT == 16) dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-            }
-            __syncwarp();
 
-            // ---- 3. keys unresolved in-thread: walk the tile's answer chain -------------
-            // Queries (in-thread prefix minima) come in non-increasing order, so the
-            // cursor only moves left.  A query is walked only when some key of the
-            // tile before this lane qualifies (lt(carry, q)), so the walk ends inside.
-            unsigned cu = 0;
-            if (umask) {
-                unsigned Q = umask & (umask - 1);
-                int k = 0;
-                T q = v[0];
-                if (lane == 0 || !lt<INCL>(carry, q)) {
-                    cu = umask;
-                } else {
-                    int c = lane * IPT - 1;
-                    int guard = 2 * WT + 64;
-                    T cv = V[swz(c)];
-                    while (true) {
-                        if (lt<INCL>(cv, q)) {
-                            O[swz(lane * IPT + k)] = tile_base + c;
-                            if (!Q) break;
-                            k = __ffs(Q) - 1;
-                            Q &= Q - 1;
-                            q = V[swz(lane * IPT + k)];
-                            if (!lt<INCL>(carry, q)) {
-                                cu = (1u << k) | Q;
-                                break;
-                            }
-                        } else {
-                            c = sNext[c];
-                            if (c < 0 || --guard < 0) {  // cannot happen while lt(carry, q)
-                                atomicOr(err, ERR_INTERNAL);
-                                cu = (1u << k) | Q;
-                                break;
-                            }
-                            cv = V[swz(c)];
+            // ---- 3. classify the keys without an in-thread answer ------------------------
+            // X: answered by an earlier lane of the tile; S: by an earlier tile of the
+            // range (the stack); D: by nothing in the range (deferred to phase 2).
+            unsigned gtb = 0, gtr = 0;
+#pragma unroll
+            for (int k = 0; k < IPT; k++) {
+                gtb |= (unsigned)lt<INCL>(before, v[k]) << k;
+                gtr |= (unsigned)lt<INCL>(rmin, v[k]) << k;
+            }
+            const unsigned xm = lane > 0 ? (umask & gtb) : 0u;
+            const unsigned sm = has_rmin ? (umask & ~xm & gtr) : 0u;
+            const unsigned dm = umask & ~xm & ~sm;
+            __syncwarp();  // the in-thread answers and suffix minima are in shared memory
+
+            // ---- 4. X keys: lane by binary lifting, then key by binary search ------------
+            const int cx = __popc(xm);
+            const int xtot = (int)__reduce_add_sync(FULL, (unsigned)cx);
+            if (xtot) {
+                // lane table: tab[k] = min of lane minima over lanes (lane - 2^k, lane]
+                T tab[5];
+                tab[0] = lmin;
+#pragma unroll
+                for (int k = 1; k < 5; k++) {
+                    const T u = __shfl_up_sync(FULL, tab[k - 1], 1 << (k - 1));
+                    tab[k] = lane >= (1 << (k - 1)) ? KeyTraits<T>::vmin(tab[k - 1], u) : tab[k - 1];
+                }
+                // One query per lane and round.  A key e of lane ql = e / IPT is an X key
+                // only when some lane before ql qualifies, so the lifting below never
+                // passes lane 0: it ends on the nearest qualifying lane p (invariant: the
+                // answer lane is <= p and after each step p - answer < 2^k).  In lane p,
+                // the suffix minima qualify on a prefix [0, j] and key j is the answer.
+                auto resolve2 = [&](int e0, bool a0, int e1, bool a1) {
+                    const int e[2] = {e0, e1};
+                    const bool act[2] = {a0, a1};
+                    T q[2];
+                    int p[2];
+#pragma unroll
+                    for (int i2 = 0; i2 < 2; i2++) {
+                        q[i2] = act[i2] ? V[swz(e[i2])] : KeyTraits<T>::pad();
+                        p[i2] = act[i2] ? e[i2] / IPT - 1 : 0;
+                    }
+#pragma unroll
+                    for (int k = 4; k >= 0; k--) {
+#pragma unroll
+                        for (int i2 = 0; i2 < 2; i2++) {
+                            const T m = __shfl_sync(FULL, tab[k], p[i2] & 31);
+                            if (act[i2] && !lt<INCL>(m, q[i2])) p[i2] -= 1 << k;
                         }
                     }
-                }
-            }
-
-            // ---- 4. keys with no answer in the tile: the range stack ----------------------
-            // The stack's top 32 entries sit one per lane; a query is one ballot
-            // (entries below a query form a prefix, the top qualifying lane wins).
-            const int win_lo = max(stk_lo, stk_top - 32);
-            const int widx = win_lo + lane;
-            const bool wvalid = widx < stk_top;
-            const T wv = wvalid ? sStkV[widx % K] : KeyTraits<T>::pad();
-            unsigned dmask = 0;
-            if (cu) {
-                const T qmax = V[swz(lane * IPT + __ffs(cu) - 1)];
-                if (!has_rmin || !lt<INCL>(rmin, qmax)) {
-                    dmask = cu;  // nothing in the range qualifies even for the largest
-                } else {
-                    unsigned m = cu;
+                    int j[2] = {0, 0};
+#pragma unroll
+                    for (int i2 = 0; i2 < 2; i2++)
+                        if (act[i2] && p[i2] < 0) {  // cannot happen (see the invariant); stay in bounds
+                            atomicOr(err, ERR_INTERNAL);
+                            p[i2] = 0;
+                        }
+#pragma unroll
+                    for (int s2 = IPT / 2; s2 > 0; s2 >>= 1) {
+#pragma unroll
+                        for (int i2 = 0; i2 < 2; i2++)
+                            if (act[i2] && lt<INCL>(sSM[swz(p[i2] * IPT + j[i2] + s2)], q[i2])) j[i2] += s2;
+                    }
+#pragma unroll
+                    for (int i2 = 0; i2 < 2; i2++)
+                        if (act[i2]) O[swz(e[i2])] = tile_base + p[i2] * IPT + j[i2];
+                };
+                const int xmax = (int)__reduce_max_sync(FULL, (unsigned)cx);
+                const int rounds = (xtot + 63) >> 6;
+                if (xmax > 2 * rounds + 1) {
+                    // spread the queries evenly: an ordered list of X keys
+                    int tot_unused;
+                    int off = warp_excl_sum(cx, tot_unused);
+                    unsigned m = xm;
                     while (m) {
                         const int k = __ffs(m) - 1;
                         m &= m - 1;
-                        const int e = lane * IPT + k;
-                        const T q = V[swz(e)];
-                        if (!lt<INCL>(rmin, q)) {
-                            dmask |= (1u << k) | m;  // queries only shrink from here on
-                            break;
-                        }
-                        int lo = stk_lo, hi = stk_top;  // first stored index that does not qualify
-                        while (lo < hi) {
-                            const int mid = (lo + hi) >> 1;
-                            if (lt<INCL>(sStkV[mid % K], q)) lo = mid + 1;
-                            else hi = mid;
-                        }
-                        if (lo > stk_lo) O[swz(e)] = sStkP[(lo - 1) % K];
-                        else dmask |= 1u << k;  // below the kept part of the stack
+                        sList[off++] = (int16_t)(lane * IPT + k);
+                    }
+                    __syncwarp();
+                    for (int b0 = 0; b0 < xtot; b0 += 64) {
+                        const bool a0 = b0 + lane < xtot, a1 = b0 + 32 + lane < xtot;
+                        resolve2(a0 ? (int)sList[b0 + lane] : 0, a0, a1 ? (int)sList[b0 + 32 + lane] : 0, a1);
+                    }
+                } else {
+                    unsigned m = xm;
+                    for (int rd = 0; rd < xmax; rd += 2) {
+                        const bool a0 = m != 0;
+                        const int k0 = a0 ? __ffs(m) - 1 : 0;
+                        m &= m - 1;
+                        const bool a1 = m != 0;
+                        const int k1 = a1 ? __ffs(m) - 1 : 0;
+                        m &= m - 1;
+                        resolve2(lane * IPT + k0, a0, lane * IPT + k1, a1);
                     }
                 }
             }
-            const int dc = (int)__reduce_add_sync(FULL, (unsigned)__popc(dmask));
-            const bool may_cap = stk_lo > 0;
 
-            // ---- 5. stack update ----------------------------------------------------------------
-            if (!last_of_range) {
+            // ---- 5. S keys: search of the range stack -------------------------------------
+            // Entries are strict suffix minima: values increase from bottom to top and
+            // the ones that qualify form a bottom part; the topmost of them answers.
+            // The top 32 entries sit one per lane (the window), so a query is one
+            // ballot.  With nothing ever dropped the bottom entry is the range minimum,
+            // which qualifies; otherwise a miss is "capped": the answer lies in the
+            // range below the kept entries and phase 2 finds it.
+            const int win_lo = max(stk_lo, stk_hi - 32);
+            const int widx = win_lo + lane;
+            const bool wvalid = widx < stk_hi;
+            const T wv = wvalid ? sStkV[widx & (K - 1)] : KeyTraits<T>::pad();
+            unsigned cm = 0;
+            {
+                const int smax = (int)__reduce_max_sync(FULL, (unsigned)__popc(sm));
+                if (smax) {
+                    const int wcnt = stk_hi - win_lo;  // window entries (uniform)
+                    const int wp = wvalid ? sStkP[widx & (K - 1)] : -1;
+                    unsigned m = sm;
+                    for (int rd = 0; rd < smax; rd++) {
+                        const bool act = m != 0;
+                        const int k = act ? __ffs(m) - 1 : 0;
+                        m &= m - 1;
+                        const T q = act ? V[swz(lane * IPT + k)] : KeyTraits<T>::pad();
+                        // topmost window entry that qualifies (they form a bottom part)
+                        int lo = -1;
+#pragma unroll
+                        for (int s2 = 32; s2 > 0; s2 >>= 1) {
+                            const int cand = lo + s2;
+                            const T wc = __shfl_sync(FULL, wv, cand & 31);
+                            if (act && cand < wcnt && lt<INCL>(wc, q)) lo = cand;
+                        }
+                        const int ap = __shfl_sync(FULL, wp, lo & 31);
+                        if (act) {
+                            int ans = lo >= 0 ? ap : -1;
+                            if (lo < 0 && win_lo > stk_lo) {  // below the window: binary search
+                                int l2 = stk_lo, h2 = win_lo;
+                                while (l2 < h2) {
+                                    const int mid = (l2 + h2) >> 1;
+                                    if (lt<INCL>(sStkV[mid & (K - 1)], q)) l2 = mid + 1;
+                                    else h2 = mid;
+                                }
+                                if (l2 > stk_lo) ans = sStkP[(l2 - 1) & (K - 1)];
+                            }
+                            if (ans >= 0) O[swz(lane * IPT + k)] = ans;
+                            else cm |= 1u << k;
+                        }
+                    }
+                    if (cm && !dropped) atomicOr(err, ERR_INTERNAL);
+                }
+            }
+
+            // ---- 6. flagged keys: deferred (D) and capped (C) -----------------------------
+            // They keep -1 in O.  The first kDefCap deferred and kCapCap capped keys of
+            // the range go to in-order lists in shared memory for phase 2; every tile also
+            // leaves its flags in global memory for the lists' overflow.
+            {
+                const unsigned fm = dm | cm;
+                const int nd = __popc(dm), nc = __popc(cm);
+                const unsigned anyf = __ballot_sync(FULL, fm != 0);
+                int dtot = 0, ctot = 0;
+                if (anyf) {
+                    const int doff = warp_excl_sum(nd, dtot);
+                    const int coff = warp_excl_sum(nc, ctot);
+                    {
+                        int idx = def_total + doff;
+                        unsigned m = dm;
+                        while (m && idx < kDefCap) {
+                            const int k = __ffs(m) - 1;
+                            m &= m - 1;
+                            sDefP[idx] = lb + k;
+                            sDefV[idx] = V[swz(lane * IPT + k)];
+                            idx++;
+                        }
+                    }
+                    {
+                        int idx = cap_total + coff;
+                        unsigned m = cm;
+                        while (m && idx < kCapCap) {
+                            const int k = __ffs(m) - 1;
+                            m &= m - 1;
+                            sCapP[idx++] = lb + k;
+                        }
+                    }
+                    // mask word w covers keys [32w, 32w + 32): lanes TPC*w .. TPC*w + TPC - 1
+                    uint32_t mw = 0;
+#pragma unroll
+                    for (int j = 0; j < TPC; j++) {
+                        const unsigned part = __shfl_sync(FULL, fm, (lane % W) * TPC + j);
+                        mw |= part << (j * IPT);
+                    }
+                    if (lane < W) __stcg(&a.s.tile_mask[(size_t)t * MW + lane], mw);
+                    def_total += dtot;
+                    cap_total += ctot;
+                }
+                if (lane == 0) __stcg(&a.s.tile_flag[t], (uint32_t)(dtot + ctot) | (ctot ? 0x80000000u : 0u));
+            }
+
+            // ---- 7. output: the whole tile, flagged keys as -1 ----------------------------
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (full) {
+                if (lane == 0) {
+                    tma_store_2d(&map_out, 0, t * W, O);
+                    bulk_commit();
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < IPT; j++) {
+                    const int e = j * 32 + lane;
+                    if (e < valid_keys) a.d_out[tile_base + e] = O[swz(e)];
+                }
+            }
+
+            // ---- 8. stack update: pop what the tile dominates, push its suffix minima ----
+            {
+                T suf = lmin;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const T nb = __shfl_down_sync(FULL, suf, o);
+                    if (lane + o < 32) suf = KeyTraits<T>::vmin(suf, nb);
+                }
+                const T after_w = __shfl_down_sync(FULL, suf, 1);  // min of the lanes after (lane < 31)
                 unsigned fmask = 0;
                 const bool has_aft = lane < 31;
-                if (!has_aft || lt<false>(tmin, after_w)) {  // else no key here beats every later key
+                if (!has_aft || lt<false>(lmin, after_w)) {  // else no key here beats every later key
                     bool has_run = has_aft;
                     T run = after_w;
 #pragma unroll
@@ -578,98 +714,51 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     }
                 }
                 const int fcnt = __popc(fmask);
-                const unsigned fl = __ballot_sync(FULL, fcnt != 0);
-                int fpre = 0, total;
-                if ((fl & (fl - 1)) == 0) {  // one lane holds every new entry
-                    total = __shfl_sync(FULL, fcnt, fl ? __ffs(fl) - 1 : 0);
-                } else {
-                    fpre = fcnt;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int nb = __shfl_up_sync(FULL, fpre, o);
-                        if (lane >= o) fpre += nb;
-                    }
-                    total = __shfl_sync(FULL, fpre, 31);
-                    fpre -= fcnt;
-                }
-                // Stored entries below the tile min survive: a prefix of the stack.
+                int total;
+                const int fpre = warp_excl_sum(fcnt, total);
+                // Entries below the tile minimum survive: a bottom part of the stack.
                 const unsigned below = __ballot_sync(FULL, wvalid && wv < tile_min_t);
                 int keep;
                 if (below == __ballot_sync(FULL, wvalid)) {
-                    keep = stk_top;  // the whole window survives, so does everything under it
+                    keep = stk_hi;  // the whole window survives, so does everything under it
                 } else if (below || win_lo == stk_lo) {
                     keep = win_lo + __popc(below);
                 } else {  // the boundary lies under the window (rare)
                     int lo = stk_lo, hi = win_lo;
                     while (lo < hi) {
                         const int mid = (lo + hi) >> 1;
-                        if (sStkV[mid % K] < tile_min_t) lo = mid + 1;
+                        if (sStkV[mid & (K - 1)] < tile_min_t) lo = mid + 1;
                         else hi = mid;
                     }
                     keep = lo;
                 }
                 __syncwarp();  // every lane has read the old stack
                 const int newtop = keep + total;
-                if (fmask) {
+                {
                     int idx = keep + fpre;
-#pragma unroll
-                    for (int k = 0; k < IPT; k++) {
-                        if ((fmask >> k) & 1u) {
-                            if (idx >= newtop - K) {
-                                sStkV[idx % K] = v[k];
-                                sStkP[idx % K] = tile_base + lane * IPT + k;
-                            }
-                            idx++;
+                    unsigned m = fmask;
+                    if (idx + fcnt <= newtop - K) m = 0;  // all of this lane's entries drop at once
+                    while (m) {
+                        const int k = __ffs(m) - 1;
+                        m &= m - 1;
+                        if (idx >= newtop - K) {
+                            sStkV[idx & (K - 1)] = V[swz(lane * IPT + k)];
+                            sStkP[idx & (K - 1)] = lb + k;
                         }
+                        idx++;
                     }
                 }
-                stk_top = newtop;
-                stk_lo = max(stk_lo, newtop - K);
+                stk_hi = newtop;
+                if (newtop - K > stk_lo) {
+                    stk_lo = newtop - K;
+                    dropped = true;
+                }
             }
 
-            // ---- 6. publish tile data, output -------------------------------------------------
-            if (lane == 0) {
-                __stcg(&tile_min_w[t], tile_min_t);
-                // bit 32: a range prefix exists; bit 33: the stack had dropped entries, so a
-                // deferred key of this tile may have its answer inside the range
-                __stcg(&a.s.tile_rpre[t], has_rmin ? ((1ull << 32) | (may_cap ? (1ull << 33) : 0ull) |
-                                                      KeyTraits<T>::bits(rmin))
-                                                   : 0ull);
-                __stcg(&a.s.tile_defcnt[t], dc);
-            }
+            // ---- 9. tile minimum, range minimum, next load ------------------------------
+            if (lane == 0) __stcg(&tile_min_w[t], tile_min_t);
             rmin = has_rmin ? KeyTraits<T>::vmin(rmin, tile_min_t) : tile_min_t;
             has_rmin = true;
-            fence_proxy_async_smem();
-            __syncwarp();
-            if (dc == 0) {
-                if (full) {
-                    if (lane == 0) {
-                        tma_store_2d(&map_out, 0, t * W, O);
-                        bulk_commit();
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < IPT; j++) {
-                        const int e = j * 32 + lane;
-                        if (e < valid_keys) a.d_out[tile_base + e] = O[swz(e)];
-                    }
-                }
-            } else if (dc < valid_keys) {
-                // mask word w covers keys [32w, 32w + 32): lanes TPC*w .. TPC*w + TPC - 1
-                uint32_t mw = 0;
-#pragma unroll
-                for (int j = 0; j < TPC; j++) {
-                    const unsigned part = __shfl_sync(FULL, dmask, (lane % W) * TPC + j);
-                    mw |= part << (j * IPT);
-                }
-#pragma unroll
-                for (int j = 0; j < W; j++) {
-                    const uint32_t wj = __shfl_sync(FULL, mw, j);
-                    const int e = j * 32 + lane;
-                    if (e < valid_keys && !((wj >> lane) & 1u)) a.d_out[tile_base + e] = O[swz(e)];
-                }
-                if (lane < W) __stcg(&a.s.tile_defmask[(size_t)t * MW + lane], mw);
-            }
             __syncwarp();
             if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
                 mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * 4));
@@ -677,182 +766,184 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
         }
 
-        // ======================= publish the range, look back =======================
-        if (lane == 0) {
-            bulk_wait_read0();
-            __stcg(&((T*)a.s.range_min)[r], rmin);
+        // ======================= publish the range, its prefix ======================
+        {  // the top of the final stack, for later ranges' deferred keys
+            const int tb = max(stk_lo, stk_hi - kTopEntries);
+            const int tc = stk_hi - tb;
+            T* top_key = (T*)a.s.top_key + (size_t)r * kTopEntries;
+            int32_t* top_pos = a.s.top_pos + (size_t)r * kTopEntries;
+            if (lane < tc) {
+                __stcg(&top_key[lane], sStkV[(tb + lane) & (K - 1)]);
+                __stcg(&top_pos[lane], sStkP[(tb + lane) & (K - 1)]);
+            }
+            if (lane == 0) __stcg(&a.s.top_cnt[r], (uint32_t)tc | ((!dropped && tb == stk_lo) ? 0x80000000u : 0u));
         }
-        __syncwarp();  // every lane's tile words before lane 0's release in range_publish
+        __syncwarp();  // every lane's words before lane 0's release in range_publish
         range_publish<T>(r, epoch, rmin, a);
         T P;
         bool has_p;
         range_prefix<T>(r, epoch, a, P, has_p);
-        __syncwarp();  // lane 0's acquire before every lane's reads of earlier ranges' words
+        if (lane == 0) {
+            bulk_wait0();       // this range's tile stores have landed ...
+            fence_proxy_async();  // ... before phase 2 overwrites flagged keys
+        }
+        __syncwarp();  // lane 0's acquire and wait before every lane's reads and writes
 
-        // ======================= phase 2: deferred keys =========================
-        // "True" deferred keys have no qualifying key in the range before them:
-        // the range's prefix minima, non-increasing, so the ones P qualifies form
-        // a prefix (pass A, in order, one monotone cursor) and every later one is
-        // -1 without reading its key (pass B).  "Capped" ones (tiles whose stack
-        // had dropped entries, rpre bit 33) have their answer inside the range.
+        // ======================= phase 2: flagged keys ===============================
         const T* tile_min_r = (const T*)a.s.tile_min;
         const T* chunk_min_r = (const T*)a.s.chunk_min;
-        const uint32_t* defmask = a.s.tile_defmask;
-        int* list = (int*)sV;  // ordered deferred offsets of one tile (the ring is idle now)
-        int stop = t1 * WT;    // first position pass B answers -1
-        {
-            int cur = -1;  // the last answer found (absolute), -1 = none yet
-            bool done = !has_p;
-            if (done) stop = t0 * WT;
-            for (int ib = 0; ib < ntr && !done; ib += 32) {
-                const int dcl = ib + lane < ntr ? __ldcg(&a.s.tile_defcnt[t0 + ib + lane]) : 0;
-                unsigned nz = __ballot_sync(FULL, dcl != 0);
-                while (nz && !done) {
-                    const int jt = __ffs(nz) - 1;
-                    nz &= nz - 1;
-                    const int t = t0 + ib + jt;
-                    const int dct = __shfl_sync(FULL, dcl, jt);
-                    const int valid = min(WT, a.n - t * WT);
-                    const uint64_t rp = __ldcg(&a.s.tile_rpre[t]);
-                    const bool has_rp = ((rp >> 32) & 1ull) != 0;
-                    const T rpv = KeyTraits<T>::from_bits((uint32_t)rp);
-                    const bool dense = dct == valid;
-                    if (!dense) {  // ordered list of the tile's deferred offsets
-                        const uint32_t wv = lane < W ? __ldcg(&defmask[(size_t)t * MW + lane]) : 0u;
-                        const int cnt = __popc(wv);
-                        int incl = cnt;
-#pragma unroll
-                        for (int o = 1; o < 32; o <<= 1) {
-                            const int nb = __shfl_up_sync(FULL, incl, o);
-                            if (lane >= o) incl += nb;
-                        }
-                        int pos = incl - cnt;
-                        uint32_t bits = wv;
-                        while (bits) {
-                            const int b = __ffs(bits) - 1;
-                            bits &= bits - 1;
-                            list[pos++] = lane * 32 + b;
-                        }
-                        __syncwarp();
-                    }
-                    for (int k0 = 0; k0 < dct && !done; k0 += 32) {
-                        const int k = k0 + lane;
-                        const bool act = k < dct;
-                        const int e = act ? (dense ? k : list[k]) : 0;
-                        const T q = act ? __ldg(&d_in[t * WT + e]) : KeyTraits<T>::pad();
-                        const bool capped = act && has_rp && lt<INCL>(rpv, q);
-                        const bool truedef = act && !capped;
-                        const bool want = truedef && lt<INCL>(P, q);
-                        unsigned wm = __ballot_sync(FULL, want);
-                        const unsigned tm = __ballot_sync(FULL, truedef);
-                        const unsigned rest = tm & ~wm;
-                        if (rest) {  // the first true key P does not qualify: all later ones are -1
-                            const int f = __ffs(rest) - 1;
-                            stop = t * WT + __shfl_sync(FULL, e, f);
-                            wm &= (1u << f) - 1u;
-                            done = true;
-                        }
-                        unsigned pend = wm;
-                        int ans = -1;
+        const int range_begin = t0 * WT;
+        auto range_end = [&](int rr) { return min(min((rr + 1) * a.tiles_per_range, a.num_tiles) * WT, a.n); };
+
+        // A. deferred keys: the range's prefix minima, non-increasing, so the ones P
+        //    qualifies form a prefix of the list and the rest keep -1.  Each answer is
+        //    in the nearest earlier range whose minimum qualifies, at the top of its
+        //    published stack (lane-parallel searches), else found by find_left.
+        bool a_done = !has_p;
+        const int nlist = min(def_total, kDefCap);
+        T win = KeyTraits<T>::pad();
+        bool win_loaded = false;
+        for (int b0 = 0; b0 < nlist && !a_done; b0 += 32) {
+            const int j = b0 + lane;
+            const bool in = j < nlist;
+            const T q = in ? sDefV[j] : KeyTraits<T>::pad();
+            const int pos = in ? sDefP[j] : 0;
+            const bool want = in && lt<INCL>(P, q);
+            if (__ballot_sync(FULL, want) != __ballot_sync(FULL, in)) a_done = true;
+            if (!__any_sync(FULL, want)) break;
+            if (!win_loaded) {  // lane i: the minimum of range r - 1 - i
+                win = r - 1 - lane >= 0 ? state_key<T>(&a.s.range_state[r - 1 - lane]) : KeyTraits<T>::pad();
+                win_loaded = true;
+            }
+            int rp = -1;
+#pragma unroll 4
+            for (int i2 = 0; i2 < 32; i2++) {
+                const T m = __shfl_sync(FULL, win, i2);
+                if (want && rp < 0 && r - 1 - i2 >= 0 && lt<INCL>(m, q)) rp = r - 1 - i2;
+            }
+            int ans = -2;  // -2: not found yet
+            if (want && rp >= 0) {
+                const uint32_t tn = __ldcg(&a.s.top_cnt[rp]);
+                const int cnt = (int)(tn & 0xffu);
+                const T* tk = (const T*)a.s.top_key + (size_t)rp * kTopEntries;
+                int lo = 0, hi = cnt;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (lt<INCL>(__ldcg(&tk[mid]), q)) lo = mid + 1;
+                    else hi = mid;
+                }
+                if (lo > 0) ans = __ldcg(&a.s.top_pos[(size_t)rp * kTopEntries + lo - 1]);
+            }
+            unsigned fb = __ballot_sync(FULL, want && ans == -2);
+            while (fb) {
+                const int f = __ffs(fb) - 1;
+                fb &= fb - 1;
+                const T qf = __shfl_sync(FULL, q, f);
+                const int rpf = __shfl_sync(FULL, rp, f);
+                const int lim = rpf >= 0 ? range_end(rpf) : range_begin;
+                const int found = find_left<T, WT, INCL>(qf, lim, d_in, tile_min_r, chunk_min_r, a);
+                if (lane == f) ans = found;
+            }
+            if (want) {
+                if (ans < 0) atomicOr(err, ERR_INTERNAL);
+                else a.d_out[pos] = ans;
+            }
+        }
+        if (!a_done && def_total > kDefCap) {
+            // A'. the list overflowed and P qualified every listed key: continue over
+            //     the tile flags after the last listed key, with a monotone cursor
+            //     (answers of non-increasing queries only move left).
+            const int from = sDefP[kDefCap - 1] + 1;
+            int cur = -1;
+            T cv = KeyTraits<T>::pad();
+            for (int t = from / WT; t < t1 && !a_done; t++) {
+                const uint32_t tf = __ldcg(&a.s.tile_flag[t]);
+                if ((tf & 0x7fffffffu) == 0) continue;
+                const bool mixed = (tf >> 31) != 0;
+                for (int w = 0; w < W && !a_done; w++) {
+                    const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
+                    const int pos = t * WT + w * 32 + lane;
+                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from);
+                    if (!pend) continue;
+                    const T q = ((pend >> lane) & 1u) ? __ldg(&d_in[pos]) : KeyTraits<T>::pad();
+                    if (mixed) {  // deferred and capped keys: a full search each
                         while (pend) {
-                            if (cur >= 0) {
-                                const T ac = __ldg(&d_in[cur]);
-                                const bool mine = (pend >> lane) & 1u;
-                                const unsigned ok = __ballot_sync(FULL, mine && lt<INCL>(ac, q));
-                                if (mine && lt<INCL>(ac, q)) ans = cur;
-                                pend &= ~ok;
-                                if (!pend) break;
-                            }
                             const int f = __ffs(pend) - 1;
-                            const T qf = __shfl_sync(FULL, q, f);
-                            const int found =
-                                find_left<T, WT, INCL>(qf, cur >= 0 ? cur : t0 * WT, d_in, tile_min_r, chunk_min_r, a);
-                            if (found < 0) {
-                                if (lane == 0) atomicOr(err, ERR_INTERNAL);
-                            } else {
-                                cur = found;
-                            }
-                            if (lane == f) ans = found < 0 ? -1 : found;
                             pend &= pend - 1;
+                            const int found = find_left<T, WT, INCL>(__shfl_sync(FULL, q, f), t * WT + w * 32 + f,
+                                                                     d_in, tile_min_r, chunk_min_r, a);
+                            if (lane == f) {
+                                if (found < -1) atomicOr(err, ERR_INTERNAL);
+                                else a.d_out[pos] = found;
+                            }
                         }
-                        if ((wm >> lane) & 1u) a.d_out[t * WT + e] = ans;
-                        __syncwarp();
+                        continue;
+                    }
+                    const unsigned wq = __ballot_sync(FULL, ((pend >> lane) & 1u) && lt<INCL>(P, q));
+                    if (wq != pend) {
+                        a_done = true;
+                        pend = wq;
+                    }
+                    while (pend) {
+                        // the pending keys, in order, up to the first one the cursor's
+                        // key does not qualify for, take the cursor
+                        const unsigned ok = __ballot_sync(FULL, ((pend >> lane) & 1u) && cur >= 0 && lt<INCL>(cv, q));
+                        const unsigned fail = pend & ~ok;
+                        const unsigned tk = fail ? (pend & ((fail & (0u - fail)) - 1u)) : pend;
+                        if ((tk >> lane) & 1u) a.d_out[pos] = cur;
+                        pend &= ~tk;
+                        if (!pend) break;
+                        const int f = __ffs(pend) - 1;
+                        const T qf = __shfl_sync(FULL, q, f);
+                        const int found = find_left<T, WT, INCL>(qf, cur >= 0 ? cur : range_begin, d_in, tile_min_r,
+                                                                 chunk_min_r, a);
+                        if (found < 0) {
+                            if (lane == 0) atomicOr(err, ERR_INTERNAL);
+                            pend = 0;
+                            a_done = true;
+                        } else {
+                            cur = found;
+                            cv = __ldg(&d_in[cur]);
+                        }
                     }
                 }
             }
         }
-        // pass B
-        bool neg_ready = false;
-        int dcl = 0;
-        uint64_t rpl = 0;
-        for (int i = 0; i < ntr; i++) {
-            if ((i & 31) == 0) {  // the next 32 tiles' counts and prefixes, one load each
-                dcl = i + lane < ntr ? __ldcg(&a.s.tile_defcnt[t0 + i + lane]) : 0;
-                rpl = i + lane < ntr ? __ldcg(&a.s.tile_rpre[t0 + i + lane]) : 0ull;
+
+        // B. capped keys: the answer is in the range, below the stack's kept part.
+        const int ncap = min(cap_total, kCapCap);
+        for (int j = 0; j < ncap; j++) {
+            const int pos = sCapP[j];
+            const int found = find_left<T, WT, INCL>(__ldg(&d_in[pos]), pos, d_in, tile_min_r, chunk_min_r, a);
+            if (lane == 0) {
+                if (found < 0) atomicOr(err, ERR_INTERNAL);
+                else a.d_out[pos] = found;
             }
-            const int t = t0 + i;
-            const int dct = __shfl_sync(FULL, dcl, i & 31);
-            if (dct == 0) continue;
-            const int valid = min(WT, a.n - t * WT);
-            const uint64_t rp = __shfl_sync(FULL, rpl, i & 31);
-            const bool may_cap_t = ((rp >> 33) & 1ull) != 0;
-            const bool has_rp = ((rp >> 32) & 1ull) != 0;
-            const T rpv = KeyTraits<T>::from_bits((uint32_t)rp);
-            const bool dense = dct == valid;
-            if (!may_cap_t) {
-                if (t * WT + valid <= stop) continue;  // pass A answered every key here
-                if (dense && t * WT >= stop) {
-                    if (tile_full(t)) {
-                        if (!neg_ready) {  // O as a -1 source buffer
-#pragma unroll
-                            for (int j = 0; j < IPT; j++) O[j * 32 + lane] = -1;
-                            fence_proxy_async_smem();
-                            __syncwarp();
-                            neg_ready = true;
+        }
+        if (cap_total > kCapCap) {
+            // B'. the capped list overflowed: every flagged key of the mixed tiles after it
+            const int from = sCapP[kCapCap - 1] + 1;
+            for (int t = from / WT; t < t1; t++) {
+                const uint32_t tf = __ldcg(&a.s.tile_flag[t]);
+                if ((tf >> 31) == 0) continue;
+                for (int w = 0; w < W; w++) {
+                    const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
+                    const int pos = t * WT + w * 32 + lane;
+                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from);
+                    while (pend) {
+                        const int f = __ffs(pend) - 1;
+                        pend &= pend - 1;
+                        const int pf = t * WT + w * 32 + f;
+                        const int found =
+                            find_left<T, WT, INCL>(__ldg(&d_in[pf]), pf, d_in, tile_min_r, chunk_min_r, a);
+                        if (lane == f) {
+                            if (found < -1) atomicOr(err, ERR_INTERNAL);
+                            else a.d_out[pf] = found;
                         }
-                        if (lane == 0) {
-                            tma_store_2d(&map_out, 0, t * W, O);
-                            bulk_commit();
-                        }
-                    } else {
-                        for (int e = lane; e < valid; e += 32) a.d_out[t * WT + e] = -1;
                     }
-                    continue;
-                }
-                // -1 at the deferred offsets >= stop, straight from the mask
-                if (lane < W) {
-                    uint32_t bits = dense ? 0xffffffffu : __ldcg(&defmask[(size_t)t * MW + lane]);
-                    const int w0 = lane * 32;
-                    if (w0 + 32 > valid) bits &= valid > w0 ? (0xffffffffu >> (32 - (valid - w0))) : 0u;
-                    while (bits) {
-                        const int b = __ffs(bits) - 1;
-                        bits &= bits - 1;
-                        const int pos = t * WT + w0 + b;
-                        if (pos >= stop) a.d_out[pos] = -1;
-                    }
-                }
-                continue;
-            }
-            // A tile that may hold capped keys: read every deferred key (rare).
-            for (int j0 = 0; j0 < valid; j0 += 32) {
-                const int e = j0 + lane;
-                bool isdef = false;
-                if (e < valid) isdef = dense || ((__ldcg(&defmask[(size_t)t * MW + (e >> 5)]) >> (e & 31)) & 1u);
-                const T q = isdef ? __ldg(&d_in[t * WT + e]) : KeyTraits<T>::pad();
-                const bool capped = isdef && has_rp && lt<INCL>(rpv, q);
-                if (isdef && !capped && t * WT + e >= stop) a.d_out[t * WT + e] = -1;
-                unsigned cm = __ballot_sync(FULL, capped);
-                while (cm) {
-                    const int f = __ffs(cm) - 1;
-                    cm &= cm - 1;
-                    const T qf = __shfl_sync(FULL, q, f);
-                    const int found = find_left<T, WT, INCL>(qf, t * WT, d_in, tile_min_r, chunk_min_r, a);
-                    if (found < 0 && lane == 0) atomicOr(err, ERR_INTERNAL);
-                    if (lane == f) a.d_out[t * WT + e] = found < 0 ? -1 : found;
                 }
             }
         }
-        if (lane == 0) bulk_wait_read0();
     }
 
     // ---- run bookkeeping: the last warp resets the control block --------------------------
@@ -891,12 +982,13 @@ size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s) {
         s->group_pre = (uint32_t*)(b + o.gpre);
         s->cta_ready = (uint32_t*)(b + o.ready);
         s->range_state = (uint64_t*)(b + o.state);
-        s->range_min = b + o.rmin;
+        s->top_key = b + o.topk;
+        s->top_pos = (int32_t*)(b + o.topp);
+        s->top_cnt = (uint32_t*)(b + o.topc);
         s->tile_min = b + o.tmin;
-        s->tile_rpre = (uint64_t*)(b + o.rpre);
         s->chunk_min = b + o.cmin;
-        s->tile_defcnt = (int32_t*)(b + o.dcnt);
-        s->tile_defmask = (uint32_t*)(b + o.dmask);
+        s->tile_flag = (uint32_t*)(b + o.flag);
+        s->tile_mask = (uint32_t*)(b + o.mask);
         s->cap_tiles = (int)o.cap_tiles;
         s->max_ranges = kMaxRanges;
     }
