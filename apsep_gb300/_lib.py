@@ -30,6 +30,7 @@ SIGNATURES = {
     "apsep_launch": ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "apsep_debug_inject": ([_vp, _i32, _u32], ctypes.c_int),
     "apsep_run_noalloc": ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
+    "apsep_run_segmented": ([_vp, _vp, _vp, _i64, _vp, _i32, _vp], ctypes.c_int),
 }
 
 NOALLOC_MAX_KEYS = 4194304  # APSEP_NOALLOC_MAX_KEYS in include/apsep.h

@@ -81,6 +81,27 @@ class Plan:
         _lib.check(st, "apsep_run")
         return out
 
+    def run_segmented(self, x: torch.Tensor, offsets: torch.Tensor, out: torch.Tensor | None = None,
+                      stream=None) -> torch.Tensor:
+        """Enqueue a batched run: segment s is x[offsets[s]:offsets[s+1]]
+        (offsets: CUDA int64, offsets[0] = 0, non-decreasing, offsets[-1] =
+        x.numel()); out[i] is relative to the start of i's segment, -1 = none."""
+        if not x.is_cuda or x.dtype != self.dtype or not x.is_contiguous():
+            raise ValueError("x must be a contiguous CUDA %s tensor" % self.dtype)
+        if (not offsets.is_cuda or offsets.dtype != torch.int64 or not offsets.is_contiguous()
+                or offsets.numel() < 2):
+            raise ValueError("offsets must be a contiguous CUDA int64 tensor of nseg + 1 >= 2 entries")
+        n = x.numel()
+        if out is None:
+            out = torch.empty(n, dtype=torch.int32, device=x.device)
+        if out.dtype != torch.int32 or not out.is_cuda or not out.is_contiguous() or out.numel() < n:
+            raise ValueError("out must be a contiguous CUDA int32 tensor of x.numel() entries")
+        st = self._lib.apsep_run_segmented(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                           n, ctypes.c_void_p(offsets.data_ptr()), offsets.numel() - 1,
+                                           ctypes.c_void_p(_stream_handle(x.device, stream)))
+        _lib.check(st, "apsep_run_segmented")
+        return out
+
     def check(self, stream=None) -> None:
         """Synchronise and raise on device-side errors of earlier runs."""
         _lib.check(self._lib.apsep_plan_check(self._h, ctypes.c_void_p(_stream_handle(self.device, stream))),
@@ -125,6 +146,23 @@ def apse(x: torch.Tensor, inclusive: bool = False, out: torch.Tensor | None = No
             plan = Plan(max(x.numel(), 1 << 16), x.dtype, device=x.device)
         _cache[key] = plan
     return plan.run(x, out=out, inclusive=inclusive)
+
+
+def apse_segmented(x: torch.Tensor, offsets: torch.Tensor, inclusive: bool = False,
+                   out: torch.Tensor | None = None) -> torch.Tensor:
+    """One call over a batch of back-to-back arrays (see Plan.run_segmented)."""
+    if not x.is_cuda:
+        raise ValueError("apse_segmented runs on CUDA tensors only (there is no CPU path)")
+    x = x.contiguous()
+    key = (x.device, x.dtype, bool(inclusive), "seg")
+    plan = _cache.get(key)
+    if plan is None or plan.capacity < x.numel():
+        if plan is not None:
+            plan.close()
+        with torch.cuda.device(x.device):
+            plan = Plan(max(x.numel(), 1 << 16), x.dtype, inclusive=inclusive, device=x.device)
+        _cache[key] = plan
+    return plan.run_segmented(x, offsets, out=out)
 
 
 # ---------------------------------------------------------------------------

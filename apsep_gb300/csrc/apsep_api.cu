@@ -184,12 +184,22 @@ apsep_status apsep_plan_set_config(apsep_plan* p, int32_t config) {
     return APSEP_OK;
 }
 
-apsep_status apsep_run_cmp(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
-                           void* stream) {
+}  // extern "C"
+
+namespace {
+
+// One run of the range engine: a single array, or (offsets != nullptr) a batch
+// of nseg segments stored back to back.
+apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                      const int64_t* offsets, int32_t nseg, void* stream) {
     if (!p || n < 0 || (cmp != APSEP_LT && cmp != APSEP_LE)) return APSEP_EINVAL;
+    if (offsets && (nseg < 1 || (uintptr_t)offsets % 8 != 0)) return APSEP_EINVAL;
     if (n == 0) return APSEP_OK;
     if (n > p->capacity || !d_in || !d_out) return APSEP_EINVAL;
     if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_EINVAL;
+    if (offsets && (ranges_overlap(offsets, (size_t)(nseg + 1) * 8, d_out, (size_t)n * 4) ||
+                    ranges_overlap(offsets, (size_t)(nseg + 1) * 8, d_in, (size_t)n * 4)))
+        return APSEP_EINVAL;
     DeviceGuard g(p->device);
     if (!g.ok) return APSEP_ECUDA;
 
@@ -217,11 +227,30 @@ apsep_status apsep_run_cmp(apsep_plan* p, const void* d_in, int32_t* d_out, int6
     a.tma_rows = rows;
     a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
     a.skip_publish_range = p->dbg_skip_range;
+    a.offsets = offsets;
+    a.nseg = offsets ? nseg : 0;
     a.s = p->rs;
     p->dbg_skip_range = -1;  // one-shot
     p->dbg_spin_limit = 0;
-    cudaError_t e = launch_range(p->dtype, cmp == APSEP_LE ? 1 : 0, p->cfg, a, mi, mo, (cudaStream_t)stream);
+    const int incl = cmp == APSEP_LE ? 1 : 0;
+    cudaError_t e = offsets ? launch_range_segmented(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
+                            : launch_range(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+apsep_status apsep_run_cmp(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                           void* stream) {
+    return run_impl(p, d_in, d_out, n, cmp, nullptr, 0, stream);
+}
+
+apsep_status apsep_run_segmented(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n,
+                                 const int64_t* d_offsets, int32_t nseg, void* stream) {
+    if (!p || !d_offsets) return APSEP_EINVAL;
+    return run_impl(p, d_in, d_out, n, (apsep_cmp)p->cmp, d_offsets, nseg, stream);
 }
 
 apsep_status apsep_run(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n, void* stream) {
@@ -246,6 +275,7 @@ apsep_status apsep_plan_check(apsep_plan* p, void* stream) {
     if (cudaMemset(p->scratch, 0, control_bytes()) != cudaSuccess ||
         cudaMemcpy(p->rs.ctr, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess)
         return APSEP_ECUDA;
+    if (err & ERR_BAD_OFFSETS) return APSEP_EINVAL;
     if (err & (ERR_LOOKBACK_TIMEOUT | ERR_TMA_TIMEOUT)) return APSEP_ETIMEOUT;
     return APSEP_EINTERNAL;
 }

@@ -12,6 +12,7 @@ enum : uint32_t {
     ERR_LOOKBACK_TIMEOUT = 1u,  // a predecessor range never published
     ERR_TMA_TIMEOUT = 2u,       // a bulk copy did not complete in time
     ERR_INTERNAL = 4u,          // a search invariant failed (bug)
+    ERR_BAD_OFFSETS = 8u,       // segment offsets not 0 = off[0] <= ... <= off[nseg] = n
 };
 
 // Look-back flag values (low 2 bits of a status word's tag).
@@ -102,6 +103,8 @@ struct RangeArgs {
     int tma_rows;            // floor(n/32): rows covered by the tensor maps (0 = no TMA)
     uint32_t spin_limit;     // bound on every device-side wait (polls)
     int skip_publish_range;  // fault injection: this range never publishes (-1 = off)
+    const int64_t* offsets;  // segmented runs: nseg + 1 segment offsets into d_in; else nullptr
+    int nseg;
     RangeScratch s;
 };
 
@@ -118,5 +121,11 @@ extern const TileConfig kTileConfigs[kNumTileConfigs];
 cudaError_t launch_range(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& map_in,
                          const CUtensorMap& map_out, cudaStream_t stream);
 cudaError_t range_prepare(int cfg);  // smem attributes + occupancy, current device
+// Segmented runs (a.offsets, a.nseg set): the same engine, answers relative to
+// each key's segment start.
+cudaError_t launch_range_segmented(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& map_in,
+                                   const CUtensorMap& map_out, cudaStream_t stream);
+cudaError_t prepare_segmented(int cfg, int* ctas_per_sm);
+cudaError_t range_max_warps(int cfg, int* warps);  // persistent warps of one launch, current device
 
 }  // namespace apsep

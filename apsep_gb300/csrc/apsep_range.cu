@@ -1,45 +1,8 @@
-// apsep_range.cu -- single-array APSE engine for sm_103a: persistent,
-// warp-independent ranges.
-//
-// One launch.  Every WARP is an independent worker: it claims a contiguous
-// RANGE of warp tiles (32 lanes x IPT keys) from an atomic counter, keeps its
-// own ring of TMA stages, its own answer buffers and its own stack in shared
-// memory, and synchronises only with __syncwarp -- there is no CTA-wide
-// barrier anywhere.
-//
-//  Phase 1, per warp tile (the next tiles' 128-byte-swizzled TMA loads stay
-//  in flight in the warp's ring):
-//   1. in-thread answers over IPT consecutive keys in registers (compare
-//      ladder) -- the in-thread step of apsepKernelSPT (src/apsep.cuh:2701-2707);
-//   2. warp prefix minima over lane minima (src/apsep.cuh:2709-2730);
-//   3. each key without an in-thread answer is classified: answered by an
-//      earlier lane of the tile (X), by an earlier tile of the range (S), or by
-//      nothing in the range (deferred);
-//   4. X keys, spread evenly over the lanes, find their lane by binary lifting
-//      over a 5-level table of lane minima held in registers and their key by
-//      binary search over that lane's suffix minima -- a fixed number of
-//      steps in place of the reference's warp-uniform pointer jumping, spine
-//      walk and cross-warp fallback (src/apsep.cuh:2734-2801);
-//   5. S keys binary-search the warp's RANGE STACK (strict suffix minima of
-//      the range's earlier tiles), in place of the reference's global
-//      min-tree descent (src/apsep.cuh:2952-2996) for every answer inside the
-//      range;
-//   6. the whole tile leaves shared memory in one TMA store, deferred keys as
-//      -1; the stack takes the tile's strict suffix minima.
-//  Then the warp publishes its range minimum and the top of its stack, and
-//  reads the exclusive prefix minimum P of the earlier ranges (one handshake
-//  per launch, see range_publish).  Every wait is bounded and reports
-//  ERR_LOOKBACK_TIMEOUT / ERR_TMA_TIMEOUT.
-//
-//  Phase 2 touches only the flagged keys.  Deferred keys are the range's
-//  prefix minima, non-increasing, so the ones P qualifies form a prefix (the
-//  reference's prefix-min early-out, src/apsep.cuh:2903-2926); each finds
-//  the nearest earlier range whose minimum qualifies and its answer at the
-//  top of that range's published stack, all lanes in parallel.  Everything
-//  else (stacks that dropped entries, lists that overflowed) falls back to a
-//  warp-cooperative search down the min hierarchy (find_left).
-#include "apsep_device.cuh"
-#include "apsep_internal.h"
+// apsep_range.cu -- host side of the range engine: scratch layout, occupancy,
+// launches of the single-array kernels (the kernel itself is in
+// apsep_range_kernel.cuh; the segmented instantiations are in
+// apsep_segmented.cu).
+#include "apsep_range_kernel.cuh"
 
 namespace apsep {
 
@@ -48,930 +11,6 @@ const TileConfig kTileConfigs[kNumTileConfigs] = {
     {8, 8},   // 8 warps per CTA, 256-key warp tiles
 };
 
-constexpr int kStages = 3;      // TMA ring depth per warp (tiles)
-constexpr int kStackCap = 128;  // range-stack entries kept per warp
-constexpr int kDefCap = 64;     // deferred keys listed in shared memory per range
-constexpr int kCapCap = 32;     // capped keys listed in shared memory per range
-
-// Shared memory of one warp.
-template <int IPT>
-struct WLayout {
-    static constexpr int WT = 32 * IPT;                              // keys per warp tile
-    static constexpr size_t kV = 0;                                   // T[S][WT], swizzled (TMA dst)
-    static constexpr size_t kO = kV + (size_t)kStages * WT * 4;       // int32[WT], swizzled (TMA src)
-    static constexpr size_t kSM = kO + (size_t)WT * 4;                // T[WT], swizzled: lane suffix minima
-    static constexpr size_t kList = kSM + (size_t)WT * 4;             // int16[WT]: X keys in order
-    static constexpr size_t kStkV = kList + (size_t)WT * 2;           // T[K]
-    static constexpr size_t kStkP = kStkV + (size_t)kStackCap * 4;    // int32[K]
-    static constexpr size_t kDefP = kStkP + (size_t)kStackCap * 4;    // int32[kDefCap]
-    static constexpr size_t kDefV = kDefP + (size_t)kDefCap * 4;      // T[kDefCap]
-    static constexpr size_t kCapP = kDefV + (size_t)kDefCap * 4;      // int32[kCapCap]
-    static constexpr size_t kBar = (kCapP + (size_t)kCapCap * 4 + 7) / 8 * 8;  // uint64[S]
-    static constexpr size_t kEnd = kBar + (size_t)kStages * 8;
-    static constexpr size_t kBytes = (kEnd + 1023) / 1024 * 1024;     // keeps every warp 1024-aligned
-    static_assert(kO % 1024 == 0 && kSM % 1024 == 0 && (WT * 4) % 1024 == 0,
-                  "swizzled buffers need 1024-byte alignment");
-};
-
-template <int IPT, int WPC>
-constexpr size_t kernel_smem_bytes() { return WLayout<IPT>::kBytes * WPC + 1024; }
-
-__device__ __forceinline__ uint32_t make_tag(uint32_t epoch, uint32_t flag) { return (epoch << 2) | flag; }
-
-// ---------------------------------------------------------------------------
-// Warp-cooperative search: the rightmost position p < limit with
-// lt(d_in[p], q), or -1 (-2 if the published minima contradict each other).
-// Descends a five-level min hierarchy, 32 entries per ballot: groups of 32
-// ranges (group_state) -> ranges (range_state) -> tiles of a range
-// (tile_min) -> 32-key chunks of a tile (chunk_min) -> keys, so an answer
-// any distance away costs a handful of dependent L2 reads.  Every range
-// before the one holding limit-1, and every group before that range's group,
-// must have published; so must the tiles and chunks below limit-1.  Reads of
-// the published arrays go to L2 (ld.cg); the keys are read-only.
-// ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ T state_key(const uint64_t* w) {
-    return KeyTraits<T>::from_bits((uint32_t)__ldcg((const unsigned long long*)w));
-}
-
-// Rightmost index i in [lo, hi] (hi - lo < 32) whose minimum qualifies, or -1.
-template <typename T, bool INCL, typename Load>
-__device__ __forceinline__ int ballot_last(int lo, int hi, T q, Load load) {
-    const int lane = threadIdx.x & 31;
-    const int i = hi - lane;
-    const bool ok = i >= lo && lt<INCL>(load(i), q);
-    const unsigned m = __ballot_sync(0xffffffffu, ok);
-    return m ? hi - (__ffs(m) - 1) : -1;
-}
-
-// Exclusive prefix sum over the warp's lanes of a count c, and the total.
-__device__ __forceinline__ int warp_excl_sum(int c, int& total) {
-    int x = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int nb = __shfl_up_sync(0xffffffffu, x, o);
-        if ((int)(threadIdx.x & 31) >= o) x += nb;
-    }
-    total = __shfl_sync(0xffffffffu, x, 31);
-    return x - c;
-}
-
-template <typename T, int B, bool INCL>
-__device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in, const T* __restrict__ tile_min,
-                                      const T* __restrict__ chunk_min, const RangeArgs& a) {
-    constexpr int W = B / 32;
-    static_assert(W <= 32, "a tile's chunks must fit one ballot");
-    const int lane = threadIdx.x & 31;
-    if (limit <= 0) return -1;
-    const int last = limit - 1;
-    const int t = last / B;
-    const int c = (last - t * B) >> 5;
-    {  // 1. the row holding limit-1, positions below limit
-        const int row = t * B + c * 32;
-        const int p = row + lane;
-        const bool ok = p < limit && lt<INCL>(__ldg(&d_in[p]), q);
-        const unsigned m = __ballot_sync(0xffffffffu, ok);
-        if (m) return row + 31 - __clz(m);
-    }
-    auto tmin = [&](int i) { return __ldcg(&tile_min[i]); };
-    const int tpr = a.tiles_per_range;
-    int s = -1;  // tile holding the answer
-    int cc = ballot_last<T, INCL>(0, c - 1, q, [&](int i) { return __ldcg(&chunk_min[(size_t)t * W + i]); });
-    if (cc >= 0) {
-        s = t;
-    } else {
-        const int R = t / tpr;
-        // 3. earlier tiles of the same range
-        for (int hi = t - 1; hi >= R * tpr && s < 0; hi -= 32) s = ballot_last<T, INCL>(R * tpr, hi, q, tmin);
-        if (s < 0) {
-            // 4. earlier ranges of the same group, then 5. earlier groups
-            auto rmin = [&](int i) { return state_key<T>(&a.s.range_state[i]); };
-            const int g = R >> 5;
-            int rr = ballot_last<T, INCL>(g * 32, R - 1, q, rmin);
-            if (rr < 0) {
-                int gg = -1;
-                for (int hi = g - 1; hi >= 0 && gg < 0; hi -= 32)
-                    gg = ballot_last<T, INCL>(0, hi, q, [&](int i) { return state_key<T>(&a.s.group_state[i]); });
-                if (gg < 0) return -1;
-                rr = ballot_last<T, INCL>(gg * 32, min(gg * 32 + 31, a.num_ranges - 1), q, rmin);
-                if (rr < 0) return -2;
-            }
-            const int rt1 = min((rr + 1) * tpr, a.num_tiles) - 1;
-            for (int hi = rt1; hi >= rr * tpr && s < 0; hi -= 32) s = ballot_last<T, INCL>(rr * tpr, hi, q, tmin);
-            if (s < 0) return -2;
-        }
-        cc = ballot_last<T, INCL>(0, W - 1, q, [&](int i) { return __ldcg(&chunk_min[(size_t)s * W + i]); });
-        if (cc < 0) return -2;
-    }
-    const int row = s * B + cc * 32;
-    const unsigned m = __ballot_sync(0xffffffffu, lt<INCL>(__ldg(&d_in[row + lane]), q));
-    return m ? row + 31 - __clz(m) : -2;
-}
-
-// ---------------------------------------------------------------------------
-// Range minima -> exclusive prefix minima.
-//
-// Ranges form groups of 32.  Publishing range r: one release store of its
-// minimum (range_state) and one acq_rel increment of its group's counter.
-// The last range of a group to finish publishes the group minimum
-// (group_state) and increments the count of finished groups; the last group
-// computes the exclusive prefix over groups (group_pre) and raises one ready
-// flag per CTA.  Range r then needs group_pre of its group plus the minima of
-// the earlier ranges of its group: two loads, no hot spot.
-//
-// Every range of a launch is resident when the launch fits the device (the
-// grid is sized from occupancy), so the ready flag always comes.  When it
-// does not come within a bound (the launch shares the device and some warps
-// have not started), range r falls back to waiting only on the groups and
-// ranges before it, all of which already run (ids are handed out in start
-// order), so no wait depends on a warp that may not start.  Every wait is
-// bounded and reports ERR_LOOKBACK_TIMEOUT when it gives up.
-// ---------------------------------------------------------------------------
-template <typename T>
-__device__ void range_publish(int r, uint32_t epoch, T rmin, const RangeArgs& a) {
-    constexpr unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int g = r >> 5;
-    const uint32_t tag = (epoch << 2) | FLAG_AGG;
-    int last = 0;
-    if (lane == 0 && r != a.skip_publish_range) {
-        // release: this range's tile words (written by all lanes, ordered by
-        // the caller's __syncwarp) before the minimum
-        st_release_u64(&a.s.range_state[r], ((uint64_t)tag << 32) | KeyTraits<T>::bits(rmin));
-        const int members = min(32, a.num_ranges - g * 32);
-        last = atom_add_acq_rel_u32(&a.s.group_cnt[g], 1u) == (uint32_t)(members - 1);
-    }
-    if (!__shfl_sync(FULL, last, 0)) return;
-    // last of its group: every member's range_state is visible (acquire above)
-    const int ri = g * 32 + lane;
-    T v = ri < a.num_ranges ? state_key<T>(&a.s.range_state[ri]) : KeyTraits<T>::pad();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = KeyTraits<T>::vmin(v, __shfl_xor_sync(FULL, v, o));
-    const int ngroups = (a.num_ranges + 31) >> 5;
-    int glast = 0;
-    if (lane == 0) {
-        a.s.group_cnt[g] = 0;  // re-armed for the next run
-        st_release_u64(&a.s.group_state[g], ((uint64_t)tag << 32) | KeyTraits<T>::bits(v));
-        glast = atom_add_acq_rel_u32(&a.s.ctr->finished, 1u) == (uint32_t)(ngroups - 1);
-    }
-    if (!__shfl_sync(FULL, glast, 0)) return;
-    // last group: exclusive prefix over the groups (at most 128, four per lane)
-    T gv[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int gi = lane * 4 + k;
-        gv[k] = gi < ngroups ? state_key<T>(&a.s.group_state[gi]) : KeyTraits<T>::pad();
-    }
-    T tot = KeyTraits<T>::vmin(KeyTraits<T>::vmin(gv[0], gv[1]), KeyTraits<T>::vmin(gv[2], gv[3]));
-    T incl = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const T u = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl = KeyTraits<T>::vmin(incl, u);
-    }
-    T run = __shfl_up_sync(FULL, incl, 1);
-    if (lane == 0) run = KeyTraits<T>::pad();  // group 0 has no prefix (never read)
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int gi = lane * 4 + k;
-        if (gi < ngroups) a.s.group_pre[gi] = KeyTraits<T>::bits(run);
-        run = KeyTraits<T>::vmin(run, gv[k]);
-    }
-    __syncwarp();
-    __threadfence();
-    for (int c = lane; c < (int)gridDim.x; c += 32) a.s.cta_ready[(size_t)c * kReadyStride] = epoch;
-}
-
-template <typename T>
-__device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bool& has_p) {
-    constexpr unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int g = r >> 5;
-    const uint32_t tag = (epoch << 2) | FLAG_AGG;
-    p = KeyTraits<T>::pad();
-    has_p = r > 0;
-    if (r == 0) return;
-    // 1. the ready flag of this CTA (one line, polled by one lane per warp)
-    int ready = 0;
-    if (lane == 0) {
-        const uint32_t bound = min(a.spin_limit, 1u << 16);
-        const uint32_t* f = &a.s.cta_ready[(size_t)blockIdx.x * kReadyStride];
-        for (uint32_t s = 0;; s++) {
-            if (ld_acquire_u32(f) == epoch) {
-                ready = 1;
-                break;
-            }
-            if (s >= bound) break;
-            __nanosleep(s < 8 ? 64 : 256);
-        }
-    }
-    __syncwarp();  // lane 0's acquire before the other lanes' loads
-    if (__shfl_sync(FULL, ready, 0)) {
-        const int ri = g * 32 + lane;
-        T m = ri < r ? state_key<T>(&a.s.range_state[ri]) : KeyTraits<T>::pad();
-        if (lane == 0 && g > 0) m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_bits(__ldcg(&a.s.group_pre[g])));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
-        p = m;
-        return;
-    }
-    // 2. fallback: wait for the earlier groups and the earlier ranges of this group
-    for (uint32_t spins = 0;; spins++) {
-        bool ok = true;
-        T m = KeyTraits<T>::pad();
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int gi = lane * 4 + k;
-            if (gi < g) {
-                const uint64_t w = ld_acquire_u64(&a.s.group_state[gi]);
-                if ((uint32_t)(w >> 32) != tag) ok = false;
-                m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_bits((uint32_t)w));
-            }
-        }
-        const int ri = g * 32 + lane;
-        if (ri < r) {
-            const uint64_t w = ld_acquire_u64(&a.s.range_state[ri]);
-            if ((uint32_t)(w >> 32) != tag) ok = false;
-            m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_bits((uint32_t)w));
-        }
-        if (__all_sync(FULL, ok)) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
-            p = m;
-            return;
-        }
-        if (spins >= a.spin_limit) {
-            if (lane == 0) atomicOr(&a.s.ctr->err, ERR_LOOKBACK_TIMEOUT);
-            return;
-        }
-        __nanosleep(spins < 128 ? 64 : 256);
-    }
-}
-
-template <typename T, int IPT, int WPC, bool INCL>
-__global__ void __launch_bounds__(WPC * 32, (IPT >= 16 ? 2 : 3))
-apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
-                 const RangeArgs a) {
-    using L = WLayout<IPT>;
-    constexpr int WT = L::WT;      // keys per warp tile
-    constexpr int W = WT / 32;     // 32-key chunks (and TMA rows) per warp tile
-    constexpr int TPC = 32 / IPT;  // lanes per chunk
-    constexpr int K = kStackCap;
-    constexpr int MW = kMaxTileKeys / 32;  // flag-mask words per tile in global
-    static_assert(IPT == 8 || IPT == 16, "IPT must be 8 or 16");
-    static_assert((K & (K - 1)) == 0, "the stack ring needs a power-of-two size");
-    constexpr unsigned FULL = 0xffffffffu;
-
-    extern __shared__ unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    unsigned char* wsm =
-        (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023) + (size_t)warp * L::kBytes;
-    T* sV = (T*)(wsm + L::kV);
-    int32_t* O = (int32_t*)(wsm + L::kO);
-    T* sSM = (T*)(wsm + L::kSM);
-    int16_t* sList = (int16_t*)(wsm + L::kList);
-    T* sStkV = (T*)(wsm + L::kStkV);
-    int32_t* sStkP = (int32_t*)(wsm + L::kStkP);
-    int32_t* sDefP = (int32_t*)(wsm + L::kDefP);
-    T* sDefV = (T*)(wsm + L::kDefV);
-    int32_t* sCapP = (int32_t*)(wsm + L::kCapP);
-    uint64_t* bar = (uint64_t*)(wsm + L::kBar);
-
-    const T* d_in = (const T*)a.d_in;
-    T* tile_min_w = (T*)a.s.tile_min;
-    T* chunk_min_w = (T*)a.s.chunk_min;
-    uint32_t* err = &a.s.ctr->err;
-
-    int r = 0;
-    uint32_t epoch = 0;
-    if (lane == 0) {
-        r = (int)atomicAdd(&a.s.ctr->range_counter, 1u);
-        epoch = ld_relaxed_u32(&a.s.ctr->epoch);
-        for (int s = 0; s < kStages; s++) mbar_init(&bar[s], 1);
-        fence_mbarrier_init();
-        fence_proxy_async_smem();
-    }
-    r = __shfl_sync(FULL, r, 0);
-    epoch = __shfl_sync(FULL, epoch, 0);
-    __syncwarp();
-
-    if (r < a.num_ranges) {
-        const int t0 = r * a.tiles_per_range;
-        const int t1 = min(t0 + a.tiles_per_range, a.num_tiles);
-        const int ntr = t1 - t0;
-        auto tile_full = [&](int t) { return a.tma_rows > 0 && (t + 1) * W <= a.tma_rows; };
-        if (lane == 0) {
-            for (int i = 0; i < kStages && i < ntr; i++)
-                if (tile_full(t0 + i)) {
-                    mbar_arrive_expect_tx(&bar[i], (uint32_t)(WT * 4));
-                    tma_load_2d(sV + (size_t)i * WT, &map_in, 0, (t0 + i) * W, &bar[i]);
-                }
-        }
-        // Range state (warp-uniform): the stack ring [stk_lo, stk_hi) of strict
-        // suffix minima, values increasing from bottom to top; whether entries were
-        // ever dropped from its bottom; the range minimum so far; flagged-key counts.
-        int stk_lo = 0, stk_hi = 0;
-        bool dropped = false;
-        bool has_rmin = false;
-        T rmin = KeyTraits<T>::pad();
-        int def_total = 0, cap_total = 0;
-
-        // ======================= phase 1: the range's tiles =======================
-        for (int i = 0; i < ntr; i++) {
-            const int t = t0 + i;
-            const int slot = i % kStages;
-            const uint32_t par = (uint32_t)((i / kStages) & 1);
-            T* V = sV + (size_t)slot * WT;
-            const bool full = tile_full(t);
-            const int tile_base = t * WT;
-            const int valid_keys = min(WT, a.n - tile_base);
-
-            if (full) {
-                if (!mbar_wait_bounded(&bar[slot], par, a.spin_limit) && lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
-            } else {
-#pragma unroll
-                for (int j = 0; j < IPT; j++) {
-                    const int e = j * 32 + lane;
-                    const int g = tile_base + e;
-                    V[swz(e)] = g < a.n ? d_in[g] : KeyTraits<T>::pad();
-                }
-            }
-            if (lane == 0) bulk_wait_read0();  // the previous tile's store has read O
-            __syncwarp();
-
-            // ---- 1. in-thread answers: compare ladder over IPT keys in registers --------
-            T v[IPT];
-#pragma unroll
-            for (int q4 = 0; q4 < IPT / 4; q4++) {
-                const uint4 rr = *reinterpret_cast<const uint4*>(&V[swz(lane * IPT + 4 * q4)]);
-                v[4 * q4 + 0] = KeyTraits<T>::from_bits(rr.x);
-                v[4 * q4 + 1] = KeyTraits<T>::from_bits(rr.y);
-                v[4 * q4 + 2] = KeyTraits<T>::from_bits(rr.z);
-                v[4 * q4 + 3] = KeyTraits<T>::from_bits(rr.w);
-            }
-            const int lb = tile_base + lane * IPT;  // position of this lane's first key
-            const int nvalid = min(max(a.n - lb, 0), IPT);
-            unsigned umask = 0;     // keys without an in-thread answer
-            bool all_inc = false;   // the whole tile increases: every key answers its predecessor
-            {
-                int res[IPT];  // absolute answers, -1 = none in the thread
-                res[0] = -1;
-                // Monotone lanes (each key answers its neighbour, or no key answers any
-                // later one) need no ladder.
-                bool adj = true, none = true;
-#pragma unroll
-                for (int k = 1; k < IPT; k++) {
-                    const bool l = lt<INCL>(v[k - 1], v[k]);
-                    adj = adj && l;
-                    none = none && !l;
-                }
-                if (__all_sync(FULL, adj || none)) {
-#pragma unroll
-                    for (int k = 1; k < IPT; k++) res[k] = adj ? lb + k - 1 : -1;
-                    // every key answers its predecessor across lane boundaries too
-                    const T prev_last = __shfl_up_sync(FULL, v[IPT - 1], 1);
-                    all_inc = __all_sync(FULL, adj && (lane == 0 || lt<INCL>(prev_last, v[0]))) && valid_keys == WT;
-                    if (all_inc && lane > 0) res[0] = lb - 1;
-                } else {
-#pragma unroll
-                    for (int k = 1; k < IPT; k++) {
-                        int rk = -1;
-#pragma unroll
-                        for (int j = 0; j < k; j++)
-                            if (lt<INCL>(v[j], v[k])) rk = lb + j;
-                        res[k] = rk;
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < IPT; k++)
-                    if (res[k] < 0 && k < nvalid) umask |= 1u << k;
-                // in-thread answers; every other key holds -1 until resolved below
-#pragma unroll
-                for (int q4 = 0; q4 < IPT / 4; q4++)
-                    *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) =
-                        make_int4(res[4 * q4], res[4 * q4 + 1], res[4 * q4 + 2], res[4 * q4 + 3]);
-            }
-            T lmin;
-            {  // suffix minima of the lane's keys (for the key search of X keys)
-                T sfx[IPT];
-                sfx[IPT - 1] = v[IPT - 1];
-#pragma unroll
-                for (int k = IPT - 2; k >= 0; k--) sfx[k] = KeyTraits<T>::vmin(v[k], sfx[k + 1]);
-                lmin = sfx[0];
-#pragma unroll
-                for (int q4 = 0; q4 < IPT / 4; q4++)
-                    *reinterpret_cast<uint4*>(&sSM[swz(lane * IPT + 4 * q4)]) =
-                        make_uint4(KeyTraits<T>::bits(sfx[4 * q4]), KeyTraits<T>::bits(sfx[4 * q4 + 1]),
-                                   KeyTraits<T>::bits(sfx[4 * q4 + 2]), KeyTraits<T>::bits(sfx[4 * q4 + 3]));
-            }
-            {
-                T cmn = lmin;
-#pragma unroll
-                for (int o = 1; o < TPC; o <<= 1) cmn = KeyTraits<T>::vmin(cmn, __shfl_xor_sync(FULL, cmn, o));
-                if ((lane & (TPC - 1)) == 0) __stcg(&chunk_min_w[(size_t)t * W + lane / TPC], cmn);
-            }
-
-            // ---- 2. warp prefix minima over lane minima ---------------------------------
-            T pre = lmin;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const T nb = __shfl_up_sync(FULL, pre, o);
-                if (lane >= o) pre = KeyTraits<T>::vmin(pre, nb);
-            }
-            const T before = __shfl_up_sync(FULL, pre, 1);  // min of the lanes before (lane > 0)
-            const T tile_min_t = __shfl_sync(FULL, pre, 31);
-
-            // ---- 3. classify the keys without an in-thread answer ------------------------
-            // X: answered by an earlier lane of the tile; S: by an earlier tile of the
-            // range (the stack); D: by nothing in the range (deferred to phase 2).
-            unsigned gtb = 0, gtr = 0;
-#pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                gtb |= (unsigned)lt<INCL>(before, v[k]) << k;
-                gtr |= (unsigned)lt<INCL>(rmin, v[k]) << k;
-            }
-            const unsigned xm = lane > 0 ? (umask & gtb) : 0u;
-            const unsigned sm = has_rmin ? (umask & ~xm & gtr) : 0u;
-            const unsigned dm = umask & ~xm & ~sm;
-            __syncwarp();  // the in-thread answers and suffix minima are in shared memory
-
-            // ---- 4. X keys: lane by binary lifting, then key by binary search ------------
-            const int cx = __popc(xm);
-            const int xtot = (int)__reduce_add_sync(FULL, (unsigned)cx);
-            if (xtot) {
-                // lane table: tab[k] = min of lane minima over lanes (lane - 2^k, lane]
-                T tab[5];
-                tab[0] = lmin;
-#pragma unroll
-                for (int k = 1; k < 5; k++) {
-                    const T u = __shfl_up_sync(FULL, tab[k - 1], 1 << (k - 1));
-                    tab[k] = lane >= (1 << (k - 1)) ? KeyTraits<T>::vmin(tab[k - 1], u) : tab[k - 1];
-                }
-                // One query per lane and round.  A key e of lane ql = e / IPT is an X key
-                // only when some lane before ql qualifies, so the lifting below never
-                // passes lane 0: it ends on the nearest qualifying lane p (invariant: the
-                // answer lane is <= p and after each step p - answer < 2^k).  In lane p,
-                // the suffix minima qualify on a prefix [0, j] and key j is the answer.
-                auto resolve2 = [&](int e0, bool a0, int e1, bool a1) {
-                    const int e[2] = {e0, e1};
-                    const bool act[2] = {a0, a1};
-                    T q[2];
-                    int p[2];
-#pragma unroll
-                    for (int i2 = 0; i2 < 2; i2++) {
-                        q[i2] = act[i2] ? V[swz(e[i2])] : KeyTraits<T>::pad();
-                        p[i2] = act[i2] ? e[i2] / IPT - 1 : 0;
-                    }
-#pragma unroll
-                    for (int k = 4; k >= 0; k--) {
-#pragma unroll
-                        for (int i2 = 0; i2 < 2; i2++) {
-                            const T m = __shfl_sync(FULL, tab[k], p[i2] & 31);
-                            if (act[i2] && !lt<INCL>(m, q[i2])) p[i2] -= 1 << k;
-                        }
-                    }
-                    int j[2] = {0, 0};
-#pragma unroll
-                    for (int i2 = 0; i2 < 2; i2++)
-                        if (act[i2] && p[i2] < 0) {  // cannot happen (see the invariant); stay in bounds
-                            atomicOr(err, ERR_INTERNAL);
-                            p[i2] = 0;
-                        }
-#pragma unroll
-                    for (int s2 = IPT / 2; s2 > 0; s2 >>= 1) {
-#pragma unroll
-                        for (int i2 = 0; i2 < 2; i2++)
-                            if (act[i2] && lt<INCL>(sSM[swz(p[i2] * IPT + j[i2] + s2)], q[i2])) j[i2] += s2;
-                    }
-#pragma unroll
-                    for (int i2 = 0; i2 < 2; i2++)
-                        if (act[i2]) O[swz(e[i2])] = tile_base + p[i2] * IPT + j[i2];
-                };
-                const int xmax = (int)__reduce_max_sync(FULL, (unsigned)cx);
-                const int rounds = (xtot + 63) >> 6;
-                if (xmax > 2 * rounds + 1) {
-                    // spread the queries evenly: an ordered list of X keys
-                    int tot_unused;
-                    int off = warp_excl_sum(cx, tot_unused);
-                    unsigned m = xm;
-                    while (m) {
-                        const int k = __ffs(m) - 1;
-                        m &= m - 1;
-                        sList[off++] = (int16_t)(lane * IPT + k);
-                    }
-                    __syncwarp();
-                    for (int b0 = 0; b0 < xtot; b0 += 64) {
-                        const bool a0 = b0 + lane < xtot, a1 = b0 + 32 + lane < xtot;
-                        resolve2(a0 ? (int)sList[b0 + lane] : 0, a0, a1 ? (int)sList[b0 + 32 + lane] : 0, a1);
-                    }
-                } else {
-                    unsigned m = xm;
-                    for (int rd = 0; rd < xmax; rd += 2) {
-                        const bool a0 = m != 0;
-                        const int k0 = a0 ? __ffs(m) - 1 : 0;
-                        m &= m - 1;
-                        const bool a1 = m != 0;
-                        const int k1 = a1 ? __ffs(m) - 1 : 0;
-                        m &= m - 1;
-                        resolve2(lane * IPT + k0, a0, lane * IPT + k1, a1);
-                    }
-                }
-            }
-
-            // ---- 5. S keys: search of the range stack -------------------------------------
-            // Entries are strict suffix minima: values increase from bottom to top and
-            // the ones that qualify form a bottom part; the topmost of them answers.
-            // The top 32 entries sit one per lane (the window), so a query is one
-            // ballot.  With nothing ever dropped the bottom entry is the range minimum,
-            // which qualifies; otherwise a miss is "capped": the answer lies in the
-            // range below the kept entries and phase 2 finds it.
-            const int win_lo = max(stk_lo, stk_hi - 32);
-            const int widx = win_lo + lane;
-            const bool wvalid = widx < stk_hi;
-            const T wv = wvalid ? sStkV[widx & (K - 1)] : KeyTraits<T>::pad();
-            unsigned cm = 0;
-            {
-                const int smax = (int)__reduce_max_sync(FULL, (unsigned)__popc(sm));
-                if (smax) {
-                    const int wcnt = stk_hi - win_lo;  // window entries (uniform)
-                    const int wp = wvalid ? sStkP[widx & (K - 1)] : -1;
-                    unsigned m = sm;
-                    for (int rd = 0; rd < smax; rd++) {
-                        const bool act = m != 0;
-                        const int k = act ? __ffs(m) - 1 : 0;
-                        m &= m - 1;
-                        const T q = act ? V[swz(lane * IPT + k)] : KeyTraits<T>::pad();
-                        // topmost window entry that qualifies (they form a bottom part)
-                        int lo = -1;
-#pragma unroll
-                        for (int s2 = 32; s2 > 0; s2 >>= 1) {
-                            const int cand = lo + s2;
-                            const T wc = __shfl_sync(FULL, wv, cand & 31);
-                            if (act && cand < wcnt && lt<INCL>(wc, q)) lo = cand;
-                        }
-                        const int ap = __shfl_sync(FULL, wp, lo & 31);
-                        if (act) {
-                            int ans = lo >= 0 ? ap : -1;
-                            if (lo < 0 && win_lo > stk_lo) {  // below the window: binary search
-                                int l2 = stk_lo, h2 = win_lo;
-                                while (l2 < h2) {
-                                    const int mid = (l2 + h2) >> 1;
-                                    if (lt<INCL>(sStkV[mid & (K - 1)], q)) l2 = mid + 1;
-                                    else h2 = mid;
-                                }
-                                if (l2 > stk_lo) ans = sStkP[(l2 - 1) & (K - 1)];
-                            }
-                            if (ans >= 0) O[swz(lane * IPT + k)] = ans;
-                            else cm |= 1u << k;
-                        }
-                    }
-                    if (cm && !dropped) atomicOr(err, ERR_INTERNAL);
-                }
-            }
-
-            // ---- 6. flagged keys: deferred (D) and capped (C) -----------------------------
-            // They keep -1 in O.  The first kDefCap deferred and kCapCap capped keys of
-            // the range go to in-order lists in shared memory for phase 2; every tile also
-            // leaves its flags in global memory for the lists' overflow.
-            {
-                const unsigned fm = dm | cm;
-                const int nd = __popc(dm), nc = __popc(cm);
-                const unsigned anyf = __ballot_sync(FULL, fm != 0);
-                int dtot = 0, ctot = 0;
-                if (anyf) {
-                    const int doff = warp_excl_sum(nd, dtot);
-                    const int coff = warp_excl_sum(nc, ctot);
-                    {
-                        int idx = def_total + doff;
-                        unsigned m = dm;
-                        while (m && idx < kDefCap) {
-                            const int k = __ffs(m) - 1;
-                            m &= m - 1;
-                            sDefP[idx] = lb + k;
-                            sDefV[idx] = V[swz(lane * IPT + k)];
-                            idx++;
-                        }
-                    }
-                    {
-                        int idx = cap_total + coff;
-                        unsigned m = cm;
-                        while (m && idx < kCapCap) {
-                            const int k = __ffs(m) - 1;
-                            m &= m - 1;
-                            sCapP[idx++] = lb + k;
-                        }
-                    }
-                    // mask word w covers keys [32w, 32w + 32): lanes TPC*w .. TPC*w + TPC - 1
-                    uint32_t mw = 0;
-#pragma unroll
-                    for (int j = 0; j < TPC; j++) {
-                        const unsigned part = __shfl_sync(FULL, fm, (lane % W) * TPC + j);
-                        mw |= part << (j * IPT);
-                    }
-                    if (lane < W) __stcg(&a.s.tile_mask[(size_t)t * MW + lane], mw);
-                    def_total += dtot;
-                    cap_total += ctot;
-                }
-                if (lane == 0) __stcg(&a.s.tile_flag[t], (uint32_t)(dtot + ctot) | (ctot ? 0x80000000u : 0u));
-            }
-
-            // ---- 7. output: the whole tile, flagged keys as -1 ----------------------------
-            fence_proxy_async_smem();
-            __syncwarp();
-            if (full) {
-                if (lane == 0) {
-                    tma_store_2d(&map_out, 0, t * W, O);
-                    bulk_commit();
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < IPT; j++) {
-                    const int e = j * 32 + lane;
-                    if (e < valid_keys) a.d_out[tile_base + e] = O[swz(e)];
-                }
-            }
-
-            // ---- 8. stack update: pop what the tile dominates, push its suffix minima ----
-            {
-                T suf = lmin;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const T nb = __shfl_down_sync(FULL, suf, o);
-                    if (lane + o < 32) suf = KeyTraits<T>::vmin(suf, nb);
-                }
-                const T after_w = __shfl_down_sync(FULL, suf, 1);  // min of the lanes after (lane < 31)
-                unsigned fmask = 0;
-                const bool has_aft = lane < 31;
-                if (!has_aft || lt<false>(lmin, after_w)) {  // else no key here beats every later key
-                    bool has_run = has_aft;
-                    T run = after_w;
-#pragma unroll
-                    for (int k = IPT - 1; k >= 0; k--) {
-                        if (!has_run || v[k] < run) fmask |= 1u << k;  // strict suffix minimum
-                        run = has_run ? KeyTraits<T>::vmin(run, v[k]) : v[k];
-                        has_run = true;
-                    }
-                }
-                const int fcnt = __popc(fmask);
-                int total;
-                const int fpre = warp_excl_sum(fcnt, total);
-                // Entries below the tile minimum survive: a bottom part of the stack.
-                const unsigned below = __ballot_sync(FULL, wvalid && wv < tile_min_t);
-                int keep;
-                if (below == __ballot_sync(FULL, wvalid)) {
-                    keep = stk_hi;  // the whole window survives, so does everything under it
-                } else if (below || win_lo == stk_lo) {
-                    keep = win_lo + __popc(below);
-                } else {  // the boundary lies under the window (rare)
-                    int lo = stk_lo, hi = win_lo;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (sStkV[mid & (K - 1)] < tile_min_t) lo = mid + 1;
-                        else hi = mid;
-                    }
-                    keep = lo;
-                }
-                __syncwarp();  // every lane has read the old stack
-                const int newtop = keep + total;
-                {
-                    int idx = keep + fpre;
-                    unsigned m = fmask;
-                    if (idx + fcnt <= newtop - K) m = 0;  // all of this lane's entries drop at once
-                    while (m) {
-                        const int k = __ffs(m) - 1;
-                        m &= m - 1;
-                        if (idx >= newtop - K) {
-                            sStkV[idx & (K - 1)] = V[swz(lane * IPT + k)];
-                            sStkP[idx & (K - 1)] = lb + k;
-                        }
-                        idx++;
-                    }
-                }
-                stk_hi = newtop;
-                if (newtop - K > stk_lo) {
-                    stk_lo = newtop - K;
-                    dropped = true;
-                }
-            }
-
-            // ---- 9. tile minimum, range minimum, next load ------------------------------
-            if (lane == 0) __stcg(&tile_min_w[t], tile_min_t);
-            rmin = has_rmin ? KeyTraits<T>::vmin(rmin, tile_min_t) : tile_min_t;
-            has_rmin = true;
-            __syncwarp();
-            if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
-                mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * 4));
-                tma_load_2d(V, &map_in, 0, (t + kStages) * W, &bar[slot]);
-            }
-        }
-
-        // ======================= publish the range, its prefix ======================
-        {  // the top of the final stack, for later ranges' deferred keys
-            const int tb = max(stk_lo, stk_hi - kTopEntries);
-            const int tc = stk_hi - tb;
-            T* top_key = (T*)a.s.top_key + (size_t)r * kTopEntries;
-            int32_t* top_pos = a.s.top_pos + (size_t)r * kTopEntries;
-            if (lane < tc) {
-                __stcg(&top_key[lane], sStkV[(tb + lane) & (K - 1)]);
-                __stcg(&top_pos[lane], sStkP[(tb + lane) & (K - 1)]);
-            }
-            if (lane == 0) __stcg(&a.s.top_cnt[r], (uint32_t)tc | ((!dropped && tb == stk_lo) ? 0x80000000u : 0u));
-        }
-        __syncwarp();  // every lane's words before lane 0's release in range_publish
-        range_publish<T>(r, epoch, rmin, a);
-        T P;
-        bool has_p;
-        range_prefix<T>(r, epoch, a, P, has_p);
-        if (lane == 0) {
-            bulk_wait0();       // this range's tile stores have landed ...
-            fence_proxy_async();  // ... before phase 2 overwrites flagged keys
-        }
-        __syncwarp();  // lane 0's acquire and wait before every lane's reads and writes
-
-        // ======================= phase 2: flagged keys ===============================
-        const T* tile_min_r = (const T*)a.s.tile_min;
-        const T* chunk_min_r = (const T*)a.s.chunk_min;
-        const int range_begin = t0 * WT;
-        auto range_end = [&](int rr) { return min(min((rr + 1) * a.tiles_per_range, a.num_tiles) * WT, a.n); };
-
-        // A. deferred keys: the range's prefix minima, non-increasing, so the ones P
-        //    qualifies form a prefix of the list and the rest keep -1.  Each answer is
-        //    in the nearest earlier range whose minimum qualifies, at the top of its
-        //    published stack (lane-parallel searches), else found by find_left.
-        bool a_done = !has_p;
-        const int nlist = min(def_total, kDefCap);
-        T win = KeyTraits<T>::pad();
-        bool win_loaded = false;
-        for (int b0 = 0; b0 < nlist && !a_done; b0 += 32) {
-            const int j = b0 + lane;
-            const bool in = j < nlist;
-            const T q = in ? sDefV[j] : KeyTraits<T>::pad();
-            const int pos = in ? sDefP[j] : 0;
-            const bool want = in && lt<INCL>(P, q);
-            if (__ballot_sync(FULL, want) != __ballot_sync(FULL, in)) a_done = true;
-            if (!__any_sync(FULL, want)) break;
-            if (!win_loaded) {  // lane i: the minimum of range r - 1 - i
-                win = r - 1 - lane >= 0 ? state_key<T>(&a.s.range_state[r - 1 - lane]) : KeyTraits<T>::pad();
-                win_loaded = true;
-            }
-            int rp = -1;
-#pragma unroll 4
-            for (int i2 = 0; i2 < 32; i2++) {
-                const T m = __shfl_sync(FULL, win, i2);
-                if (want && rp < 0 && r - 1 - i2 >= 0 && lt<INCL>(m, q)) rp = r - 1 - i2;
-            }
-            int ans = -2;  // -2: not found yet
-            if (want && rp >= 0) {
-                const uint32_t tn = __ldcg(&a.s.top_cnt[rp]);
-                const int cnt = (int)(tn & 0xffu);
-                const T* tk = (const T*)a.s.top_key + (size_t)rp * kTopEntries;
-                int lo = 0, hi = cnt;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (lt<INCL>(__ldcg(&tk[mid]), q)) lo = mid + 1;
-                    else hi = mid;
-                }
-                if (lo > 0) ans = __ldcg(&a.s.top_pos[(size_t)rp * kTopEntries + lo - 1]);
-            }
-            unsigned fb = __ballot_sync(FULL, want && ans == -2);
-            while (fb) {
-                const int f = __ffs(fb) - 1;
-                fb &= fb - 1;
-                const T qf = __shfl_sync(FULL, q, f);
-                const int rpf = __shfl_sync(FULL, rp, f);
-                const int lim = rpf >= 0 ? range_end(rpf) : range_begin;
-                const int found = find_left<T, WT, INCL>(qf, lim, d_in, tile_min_r, chunk_min_r, a);
-                if (lane == f) ans = found;
-            }
-            if (want) {
-                if (ans < 0) atomicOr(err, ERR_INTERNAL);
-                else a.d_out[pos] = ans;
-            }
-        }
-        if (!a_done && def_total > kDefCap) {
-            // A'. the list overflowed and P qualified every listed key: continue over
-            //     the tile flags after the last listed key, with a monotone cursor
-            //     (answers of non-increasing queries only move left).
-            const int from = sDefP[kDefCap - 1] + 1;
-            int cur = -1;
-            T cv = KeyTraits<T>::pad();
-            for (int t = from / WT; t < t1 && !a_done; t++) {
-                const uint32_t tf = __ldcg(&a.s.tile_flag[t]);
-                if ((tf & 0x7fffffffu) == 0) continue;
-                const bool mixed = (tf >> 31) != 0;
-                for (int w = 0; w < W && !a_done; w++) {
-                    const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
-                    const int pos = t * WT + w * 32 + lane;
-                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from);
-                    if (!pend) continue;
-                    const T q = ((pend >> lane) & 1u) ? __ldg(&d_in[pos]) : KeyTraits<T>::pad();
-                    if (mixed) {  // deferred and capped keys: a full search each
-                        while (pend) {
-                            const int f = __ffs(pend) - 1;
-                            pend &= pend - 1;
-                            const int found = find_left<T, WT, INCL>(__shfl_sync(FULL, q, f), t * WT + w * 32 + f,
-                                                                     d_in, tile_min_r, chunk_min_r, a);
-                            if (lane == f) {
-                                if (found < -1) atomicOr(err, ERR_INTERNAL);
-                                else a.d_out[pos] = found;
-                            }
-                        }
-                        continue;
-                    }
-                    const unsigned wq = __ballot_sync(FULL, ((pend >> lane) & 1u) && lt<INCL>(P, q));
-                    if (wq != pend) {
-                        a_done = true;
-                        pend = wq;
-                    }
-                    while (pend) {
-                        // the pending keys, in order, up to the first one the cursor's
-                        // key does not qualify for, take the cursor
-                        const unsigned ok = __ballot_sync(FULL, ((pend >> lane) & 1u) && cur >= 0 && lt<INCL>(cv, q));
-                        const unsigned fail = pend & ~ok;
-                        const unsigned tk = fail ? (pend & ((fail & (0u - fail)) - 1u)) : pend;
-                        if ((tk >> lane) & 1u) a.d_out[pos] = cur;
-                        pend &= ~tk;
-                        if (!pend) break;
-                        const int f = __ffs(pend) - 1;
-                        const T qf = __shfl_sync(FULL, q, f);
-                        const int found = find_left<T, WT, INCL>(qf, cur >= 0 ? cur : range_begin, d_in, tile_min_r,
-                                                                 chunk_min_r, a);
-                        if (found < 0) {
-                            if (lane == 0) atomicOr(err, ERR_INTERNAL);
-                            pend = 0;
-                            a_done = true;
-                        } else {
-                            cur = found;
-                            cv = __ldg(&d_in[cur]);
-                        }
-                    }
-                }
-            }
-        }
-
-        // B. capped keys: the answer is in the range, below the stack's kept part.
-        const int ncap = min(cap_total, kCapCap);
-        for (int j = 0; j < ncap; j++) {
-            const int pos = sCapP[j];
-            const int found = find_left<T, WT, INCL>(__ldg(&d_in[pos]), pos, d_in, tile_min_r, chunk_min_r, a);
-            if (lane == 0) {
-                if (found < 0) atomicOr(err, ERR_INTERNAL);
-                else a.d_out[pos] = found;
-            }
-        }
-        if (cap_total > kCapCap) {
-            // B'. the capped list overflowed: every flagged key of the mixed tiles after it
-            const int from = sCapP[kCapCap - 1] + 1;
-            for (int t = from / WT; t < t1; t++) {
-                const uint32_t tf = __ldcg(&a.s.tile_flag[t]);
-                if ((tf >> 31) == 0) continue;
-                for (int w = 0; w < W; w++) {
-                    const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
-                    const int pos = t * WT + w * 32 + lane;
-                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from);
-                    while (pend) {
-                        const int f = __ffs(pend) - 1;
-                        pend &= pend - 1;
-                        const int pf = t * WT + w * 32 + f;
-                        const int found =
-                            find_left<T, WT, INCL>(__ldg(&d_in[pf]), pf, d_in, tile_min_r, chunk_min_r, a);
-                        if (lane == f) {
-                            if (found < -1) atomicOr(err, ERR_INTERNAL);
-                            else a.d_out[pf] = found;
-                        }
-                    }
-                }
-            }
-        }
-    }
-
-    // ---- run bookkeeping: the last warp resets the control block --------------------------
-    __syncwarp();
-    int last = 0;
-    if (lane == 0) {
-        __threadfence();
-        const uint32_t prev = atomicAdd(&a.s.ctr->done, 1u);
-        last = prev == gridDim.x * WPC - 1;
-        if (last) {
-            a.s.ctr->range_counter = 0;
-            a.s.ctr->done = 0;
-            a.s.ctr->finished = 0;
-            a.s.ctr->epoch = epoch >= EPOCH_LIMIT ? 1u : epoch + 1u;
-            __threadfence();
-        }
-    }
-    last = __shfl_sync(FULL, last, 0);
-    if (last && epoch >= EPOCH_LIMIT) {  // once per 2^30 runs: stale words could alias
-        for (int i = lane; i < a.s.max_ranges; i += 32) a.s.range_state[i] = 0;
-        for (int i = lane; i < a.s.max_ranges / 32; i += 32) a.s.group_state[i] = 0;
-        for (int i = lane; i < kMaxCtas; i += 32) a.s.cta_ready[(size_t)i * kReadyStride] = 0;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Host side.
-// ---------------------------------------------------------------------------
 size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s) {
     const ScratchOffsets o = scratch_offsets(capacity);
     if (base && s) {
@@ -1000,52 +39,16 @@ constexpr int kMaxDev = 64;
 int g_warps[kMaxDev][kNumTileConfigs];  // resident warps per device and configuration
 }
 
-template <typename T, int IPT, int WPC, bool INCL>
-static cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo, cudaStream_t st,
-                            int max_warps) {
-    constexpr size_t smem = kernel_smem_bytes<IPT, WPC>();
-    int tpr = (a.num_tiles + max_warps - 1) / max_warps;
-    if (tpr < 1) tpr = 1;
-    a.tiles_per_range = tpr;
-    a.num_ranges = (a.num_tiles + tpr - 1) / tpr;
-    const int ctas = (a.num_ranges + WPC - 1) / WPC;
-    apse_warp_kernel<T, IPT, WPC, INCL><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
-    return cudaGetLastError();
-}
-
-template <typename T, int IPT, int WPC, bool INCL>
-static cudaError_t prepare_t(int* ctas_per_sm) {
-    constexpr size_t smem = kernel_smem_bytes<IPT, WPC>();
-    auto k = apse_warp_kernel<T, IPT, WPC, INCL>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, WPC * 32, smem);
-    if (e != cudaSuccess) return e;
-    if (*ctas_per_sm == 0 || n < *ctas_per_sm) *ctas_per_sm = n;
-    return cudaSuccess;
-}
-
 cudaError_t range_prepare(int cfg) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDev || cfg < 0 || cfg >= kNumTileConfigs) return cudaErrorInvalidValue;
-    int per_sm = 0;
-#define P_(IPT, WPC)                                                                   \
-    {                                                                                  \
-        cudaError_t rr[4] = {prepare_t<int32_t, IPT, WPC, false>(&per_sm),             \
-                             prepare_t<int32_t, IPT, WPC, true>(&per_sm),              \
-                             prepare_t<float, IPT, WPC, false>(&per_sm),               \
-                             prepare_t<float, IPT, WPC, true>(&per_sm)};               \
-        for (int q = 0; q < 4; q++)                                                    \
-            if (rr[q] != cudaSuccess) return rr[q];                                    \
-    }
-    switch (cfg) {
-    case 0: P_(16, 8); break;
-    case 1: P_(8, 8); break;
-    }
-#undef P_
+    int per_sm = 0;  // the smallest over both modes, so a segmented run fits too
+    e = prepare_mode<false>(cfg, &per_sm);
+    if (e != cudaSuccess) return e;
+    e = prepare_segmented(cfg, &per_sm);
+    if (e != cudaSuccess) return e;
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
@@ -1056,8 +59,7 @@ cudaError_t range_prepare(int cfg) {
     return cudaSuccess;
 }
 
-cudaError_t launch_range(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo,
-                         cudaStream_t st) {
+cudaError_t range_max_warps(int cfg, int* warps) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -1066,20 +68,18 @@ cudaError_t launch_range(int dtype, int incl, int cfg, RangeArgs& a, const CUten
         e = range_prepare(cfg);
         if (e != cudaSuccess) return e;
     }
-    const int max_warps = g_warps[dev][cfg];
-#define L_(IPT, WPC)                                                                        \
-    if (dtype == 0)                                                                         \
-        return incl ? launch_t<int32_t, IPT, WPC, true>(a, mi, mo, st, max_warps)           \
-                    : launch_t<int32_t, IPT, WPC, false>(a, mi, mo, st, max_warps);         \
-    else                                                                                    \
-        return incl ? launch_t<float, IPT, WPC, true>(a, mi, mo, st, max_warps)             \
-                    : launch_t<float, IPT, WPC, false>(a, mi, mo, st, max_warps);
-    switch (cfg) {
-    case 0: L_(16, 8);
-    case 1: L_(8, 8);
-    }
-#undef L_
-    return cudaErrorInvalidValue;
+    *warps = g_warps[dev][cfg];
+    return cudaSuccess;
+}
+
+cudaError_t launch_range(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo,
+                         cudaStream_t st) {
+    int max_warps = 0;
+    const cudaError_t e = range_max_warps(cfg, &max_warps);
+    if (e != cudaSuccess) return e;
+    a.offsets = nullptr;
+    a.nseg = 0;
+    return launch_mode<false>(dtype, incl, cfg, a, mi, mo, st, max_warps);
 }
 
 }  // namespace apsep

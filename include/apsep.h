@@ -92,8 +92,22 @@ apsep_status apsep_run(apsep_plan* plan, const void* d_in, int32_t* d_out, int64
 apsep_status apsep_run_cmp(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
                            void* stream);
 
+/* Batched segmented run: nseg arrays stored back to back in d_in[0..n),
+ * segment s being d_in[d_offsets[s] .. d_offsets[s+1]), all in ONE launch.
+ * d_out[i] is the index, relative to the start of i's segment, of the nearest
+ * earlier key of the same segment that qualifies (plan comparator), else -1.
+ * d_offsets: device array of nseg + 1 int64, 8-byte aligned, d_offsets[0] = 0,
+ * non-decreasing, d_offsets[nseg] = n (empty segments allowed); a violation of
+ * the end points is detected on the device and reported by apsep_plan_check
+ * as APSEP_EINVAL.  Asynchronous, no allocation, graph-capturable, like
+ * apsep_run.  No counterpart in the reference (its entry points take one
+ * array); it replaces a loop of runSPT calls, one per array. */
+apsep_status apsep_run_segmented(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n,
+                                 const int64_t* d_offsets, int32_t nseg, void* stream);
+
 /* Synchronise `stream` and report device-side errors of earlier runs on this
- * plan (APSEP_ETIMEOUT / APSEP_EINTERNAL), clearing them. */
+ * plan (APSEP_ETIMEOUT / APSEP_EINTERNAL, APSEP_EINVAL for bad segment
+ * offsets), clearing them. */
 apsep_status apsep_plan_check(apsep_plan* plan, void* stream);
 
 /* Plan facts (capacity, scratch bytes, tile size, configuration). */
