@@ -61,8 +61,7 @@ struct WLayout {
     static constexpr size_t kStkP = kStkV + (size_t)kStackCap * 4;    // int32[K]
     static constexpr size_t kDefP = kStkP + (size_t)kStackCap * 4;    // int32[kDefCap]
     static constexpr size_t kDefV = kDefP + (size_t)kDefCap * 4;      // T[kDefCap]
-    static constexpr size_t kDefS = kDefV + (size_t)kDefCap * 4;      // int32[kDefCap]: segment starts
-    static constexpr size_t kCapP = kDefS + (size_t)kDefCap * 4;      // int32[kCapCap]
+    static constexpr size_t kCapP = kDefV + (size_t)kDefCap * 4;      // int32[kCapCap]
     static constexpr size_t kCapS = kCapP + (size_t)kCapCap * 4;      // int32[kCapCap]: segment starts
     static constexpr size_t kBar = (kCapS + (size_t)kCapCap * 4 + 7) / 8 * 8;  // uint64[S]
     static constexpr size_t kEnd = kBar + (size_t)kStages * 8;
@@ -358,7 +357,6 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     int32_t* sDefP = (int32_t*)(wsm + L::kDefP);
     T* sDefV = (T*)(wsm + L::kDefV);
     int32_t* sCapP = (int32_t*)(wsm + L::kCapP);
-    int32_t* sDefS = (int32_t*)(wsm + L::kDefS);
     int32_t* sCapS = (int32_t*)(wsm + L::kCapS);
     uint64_t* bar = (uint64_t*)(wsm + L::kBar);
 
@@ -403,12 +401,15 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         // Segmented runs (warp-uniform): the segment at the cursor, its start and
         // the next segment start.
         int seg_cur = 0, cur_start = 0, next_b = INT_MAX;
+        int first_start = 0, first_end = INT_MAX;  // the segment holding the range's first key
         if constexpr (SEG) {
             if (r == 0 && lane == 0 && (a.offsets[0] != 0 || a.offsets[a.nseg] != (int64_t)a.n))
                 atomicOr(err, ERR_BAD_OFFSETS);
             seg_cur = seg_find(a.offsets, a.nseg, t0 * WT, err);
             cur_start = (int)min(max(__ldg(&a.offsets[seg_cur]), (int64_t)0), (int64_t)INT_MAX);
             next_b = (int)min(max(__ldg(&a.offsets[seg_cur + 1]), (int64_t)0), (int64_t)INT_MAX);
+            first_start = cur_start;
+            first_end = next_b;
         }
 
         // ======================= phase 1: the range's tiles =======================
@@ -570,7 +571,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             const unsigned xm = lane > 0 ? (umask & gtb) : 0u;
             const unsigned sm = has_rmin ? (umask & ~xm & gtr) : 0u;
-            const unsigned dm = umask & ~xm & ~sm;
+            unsigned dm = umask & ~xm & ~sm;
+            if constexpr (SEG) {
+                // Nothing in the range qualifies for a deferred key; if its segment
+                // starts inside the range, -1 is its final answer.  Only keys of the
+                // segment holding the range's first key stay deferred.
+                if (lb + IPT > first_end) dm &= lb >= first_end ? 0u : ((1u << (first_end - lb)) - 1u);
+            }
             __syncwarp();  // the in-thread answers and suffix minima are in shared memory
 
             // ---- 4. X keys: lane by binary lifting, then key by binary search ------------
@@ -727,7 +734,6 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             m &= m - 1;
                             sDefP[idx] = lb + k;
                             sDefV[idx] = V[swz(lane * IPT + k)];
-                            if constexpr (SEG) sDefS[idx] = seg_of(k);
                             idx++;
                         }
                     }
@@ -900,9 +906,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             const bool in = j < nlist;
             const T q = in ? sDefV[j] : KeyTraits<T>::pad();
             const int pos = in ? sDefP[j] : 0;
-            const int sst = SEG && in ? sDefS[j] : 0;
-            // (a segment that starts inside this range has nothing before the range)
-            const bool want = in && lt<INCL>(P, q) && (!SEG || sst < range_begin);
+            const bool want = in && lt<INCL>(P, q);  // (segmented: all of the range's first segment)
             if (__ballot_sync(FULL, want) != __ballot_sync(FULL, in)) a_done = true;
             if (!__any_sync(FULL, want)) break;
             if (!win_loaded) {  // lane i: the minimum of range r - 1 - i
@@ -940,7 +944,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             if (want) {
                 if (ans < 0) atomicOr(err, ERR_INTERNAL);
-                else a.d_out[pos] = SEG ? seg_rel(ans, sst) : ans;
+                else a.d_out[pos] = SEG ? seg_rel(ans, first_start) : ans;
             }
         }
         if (!a_done && def_total > kDefCap) {
@@ -960,19 +964,15 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from);
                     if (!pend) continue;
                     const T q = ((pend >> lane) & 1u) ? __ldg(&d_in[pos]) : KeyTraits<T>::pad();
-                    if (mixed || SEG) {  // a full search each (capped keys, or segment starts to look up)
-                        while (pend && !a_done) {
+                    if (mixed) {  // deferred and capped keys: a full search each
+                        while (pend) {
                             const int f = __ffs(pend) - 1;
                             pend &= pend - 1;
                             const int pf = t * WT + w * 32 + f;
-                            const T qf = __shfl_sync(FULL, q, f);
+                            const int found = find_left<T, WT, INCL>(__shfl_sync(FULL, q, f), pf, d_in, tile_min_r,
+                                                                     chunk_min_r, a);
                             int sf = 0;
                             if constexpr (SEG) sf = (int)__ldg(&a.offsets[seg_find(a.offsets, a.nseg, pf, err)]);
-                            if (!mixed && (!lt<INCL>(P, qf) || (SEG && sf >= range_begin))) {
-                                a_done = true;  // deferred keys only shrink: the rest keep -1
-                                break;
-                            }
-                            const int found = find_left<T, WT, INCL>(qf, pf, d_in, tile_min_r, chunk_min_r, a);
                             if (lane == f) {
                                 if (found < -1) atomicOr(err, ERR_INTERNAL);
                                 else a.d_out[pos] = SEG ? seg_rel(found, sf) : found;
@@ -991,7 +991,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         const unsigned ok = __ballot_sync(FULL, ((pend >> lane) & 1u) && cur >= 0 && lt<INCL>(cv, q));
                         const unsigned fail = pend & ~ok;
                         const unsigned tk = fail ? (pend & ((fail & (0u - fail)) - 1u)) : pend;
-                        if ((tk >> lane) & 1u) a.d_out[pos] = cur;
+                        if ((tk >> lane) & 1u) a.d_out[pos] = SEG ? seg_rel(cur, first_start) : cur;
                         pend &= ~tk;
                         if (!pend) break;
                         const int f = __ffs(pend) - 1;
