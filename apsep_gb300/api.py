@@ -34,7 +34,10 @@ class Plan:
     """A run plan: device scratch for arrays of up to `capacity` keys."""
 
     def __init__(self, capacity: int, dtype: torch.dtype = torch.int32, inclusive: bool = False,
-                 device=None):
+                 device=None, tuning="default"):
+        """tuning: an autotune.Table (configuration per size class), "default"
+        for the table shipped for GB300 when present, or None for the
+        plan's fixed configuration (set_config)."""
         if dtype not in _DTYPES:
             raise TypeError("keys must be torch.int32 or torch.float32, got %s" % dtype)
         self._lib = _lib.load()
@@ -44,6 +47,11 @@ class Plan:
         self.inclusive = bool(inclusive)
         self.capacity = int(capacity)
         self._h = ctypes.c_void_p()
+        self._cfg = 0
+        if tuning == "default":
+            from . import autotune
+            tuning = autotune.load()
+        self._tuning = tuning
         with torch.cuda.device(self.device):
             _lib.check(self._lib.apsep_plan_create(ctypes.byref(self._h), _DTYPES[dtype],
                                                    _lib.LE if inclusive else _lib.LT, self.capacity),
@@ -60,7 +68,18 @@ class Plan:
         return inf
 
     def set_config(self, config: int) -> None:
+        """Fix the kernel configuration (turns per-size tuning off)."""
         _lib.check(self._lib.apsep_plan_set_config(self._h, int(config)), "apsep_plan_set_config")
+        self._cfg = int(config)
+        self._tuning = None
+
+    def _tune_for(self, n: int) -> None:
+        if self._tuning is None:
+            return
+        cfg = self._tuning.config_for(n)
+        if cfg is not None and cfg != self._cfg:
+            _lib.check(self._lib.apsep_plan_set_config(self._h, int(cfg)), "apsep_plan_set_config")
+            self._cfg = cfg
 
     def run(self, x: torch.Tensor, out: torch.Tensor | None = None, n: int | None = None,
             inclusive: bool | None = None, stream=None) -> torch.Tensor:
@@ -75,6 +94,7 @@ class Plan:
         if n > x.numel() or n > out.numel():
             raise ValueError("n exceeds the buffers")
         incl = self.inclusive if inclusive is None else bool(inclusive)
+        self._tune_for(n)
         st = self._lib.apsep_run_cmp(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
                                      n, _lib.LE if incl else _lib.LT,
                                      ctypes.c_void_p(_stream_handle(x.device, stream)))
@@ -96,6 +116,7 @@ class Plan:
             out = torch.empty(n, dtype=torch.int32, device=x.device)
         if out.dtype != torch.int32 or not out.is_cuda or not out.is_contiguous() or out.numel() < n:
             raise ValueError("out must be a contiguous CUDA int32 tensor of x.numel() entries")
+        self._tune_for(n)
         st = self._lib.apsep_run_segmented(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
                                            n, ctypes.c_void_p(offsets.data_ptr()), offsets.numel() - 1,
                                            ctypes.c_void_p(_stream_handle(x.device, stream)))

@@ -1,0 +1,126 @@
+"""Autotuner: the kernel configuration per size class, measured on this GPU.
+
+The engine has one tunable knob, the kernel configuration (warps per CTA x
+keys per lane, `apsep_num_configs()` of them; there is no cluster dimension:
+ranges are warp-independent).  A size class is floor(log2(n)); the tuner
+times every configuration on seeded synthetic arrays of that size (uniform,
+descending and ascending keys, the single-array benchmark's inputs), keeps the
+one with the lowest total time, and stores {class: config} in a table.  A
+Plan (or apse / the server) given a table picks the configuration per call:
+
+    table = autotune.tune(dtype=torch.int32, classes=range(14, 27))
+    autotune.save(table, "tuning.json")
+    plan = Plan(n, torch.int32, tuning=autotune.load("tuning.json"))
+
+The package ships the table measured on GB300 (tuning_gb300.json), used by
+default when present.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import torch
+
+from . import _lib
+
+DEFAULT_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_gb300.json")
+
+
+def size_class(n: int) -> int:
+    return max(int(n), 1).bit_length() - 1
+
+
+def num_configs() -> int:
+    return int(_lib.load().apsep_num_configs())
+
+
+def config_shape(config: int) -> tuple[int, int]:
+    import ctypes
+    t, k = ctypes.c_int32(), ctypes.c_int32()
+    _lib.check(_lib.load().apsep_config_shape(int(config), ctypes.byref(t), ctypes.byref(k)), "apsep_config_shape")
+    return int(t.value), int(k.value)
+
+
+class Table:
+    """{size class: configuration}; classes outside the table use the nearest one."""
+
+    def __init__(self, entries: dict[int, int], device_name: str = ""):
+        self.entries = {int(k): int(v) for k, v in entries.items()}
+        self.device_name = device_name
+
+    def config_for(self, n: int) -> int | None:
+        if not self.entries:
+            return None
+        c = size_class(n)
+        best = min(self.entries, key=lambda k: (abs(k - c), k))
+        return self.entries[best]
+
+    def to_json(self) -> dict:
+        return {"device": self.device_name, "classes": {str(k): v for k, v in sorted(self.entries.items())}}
+
+    @staticmethod
+    def from_json(d: dict) -> "Table":
+        return Table({int(k): int(v) for k, v in d.get("classes", {}).items()}, d.get("device", ""))
+
+
+def save(table: Table, path: str) -> None:
+    with open(path, "w") as f:
+        json.dump(table.to_json(), f, indent=1)
+
+
+def load(path: str = DEFAULT_TABLE) -> Table | None:
+    if not os.path.isfile(path):
+        return None
+    with open(path) as f:
+        return Table.from_json(json.load(f))
+
+
+def _inputs(n: int, dtype: torch.dtype, device) -> list[torch.Tensor]:
+    g = torch.Generator(device=device)
+    g.manual_seed(1000 + n)
+    uni = torch.randint(0, 1 << 31, (n,), generator=g, device=device, dtype=torch.int64)
+    xs = [uni.to(torch.int32), torch.arange(n - 1, -1, -1, device=device, dtype=torch.int32),
+          torch.arange(n, device=device, dtype=torch.int32)]
+    if dtype == torch.float32:
+        xs = [x.to(torch.float32) for x in xs]
+    return xs
+
+
+def tune(dtype: torch.dtype = torch.int32, classes=range(14, 27), reps: int = 5, inclusive: bool = False,
+         device=None, verbose: bool = False) -> Table:
+    """Time every configuration at n = 2^class for each class; returns the table."""
+    from .api import Plan
+
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else torch.device(device).index or 0)
+    classes = list(classes)
+    nmax = 1 << max(classes)
+    plan = Plan(nmax, dtype, inclusive=inclusive, device=dev)
+    out = torch.empty(nmax, dtype=torch.int32, device=dev)
+    entries = {}
+    try:
+        for c in classes:
+            n = 1 << c
+            xs = _inputs(n, dtype, dev)
+            best, best_t = 0, float("inf")
+            for cfg in range(num_configs()):
+                plan.set_config(cfg)
+                for x in xs:  # warm-up
+                    plan.run(x, out=out[:n])
+                torch.cuda.synchronize(dev)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    for x in xs:
+                        plan.run(x, out=out[:n])
+                e1.record()
+                plan.check()
+                t = e0.elapsed_time(e1)
+                if verbose:
+                    print("class %d config %d: %.1f us per run" % (c, cfg, t * 1e3 / (reps * len(xs))))
+                if t < best_t:
+                    best, best_t = cfg, t
+            entries[c] = best
+    finally:
+        plan.close()
+    return Table(entries, torch.cuda.get_device_name(dev))

@@ -27,6 +27,19 @@ Multi-GPU (torchrun, one rank per GPU): the path does not shard, so every
 rank runs independent replicas of the same workload ("weak" scaling); value
 is all ranks' useful bytes over the slowest rank's time.
 
+Extra objects on the same line (one GPU only; --no-extras skips them):
+  batched    4096 arrays, log-uniform lengths in [32, 2^20] (4.1e8 keys), in
+             one apsep_run_segmented launch vs a loop of one apsep_run per
+             array on one stream; useful bytes 8*sum(L) + 8*(S+1).
+  served     the serving loop (apsep_gb300.serve): requests with log-uniform
+             lengths in [2^10, 2^24], int32 / float32 50/50, host keys in and
+             answers out through device-resident pools within an 8 GiB HBM
+             budget.  Saturated throughput against the plain per-request loop,
+             then p50/p99 latency at a Poisson offered load of half the
+             server's saturated rate.
+  sweep      single-array useful GB/s and roofline fraction for N = 2^14 ..
+             2^30 (every second power of two), uniform and descending keys.
+
 --impl reference times the reference's sequential CPU algorithm (the oracle
 port of cpuApsep, src/main.cu:102-113) on the host cores, all threads busy on
 independent arrays, same workload, metric and units.
@@ -67,6 +80,20 @@ def make_inputs(n: int = N, seed: int = 20250325) -> dict[str, np.ndarray]:
 
 def useful_gbs(n: int, seconds: float, count: int = 1) -> float:
     return 2.0 * n * 4 * count / seconds / 1e9
+
+
+def max_over_ranks(values: list, dist=None, device="cpu") -> list:
+    """Each value's maximum over the ranks (the slowest replica's times)."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def whole_job_gbs(n: int, slowest_ms: float, steps: int, world: int) -> float:
+    """All ranks' useful bytes over the slowest rank's time (weak scaling: replicas)."""
+    return useful_gbs(n, slowest_ms / 1e3, steps * world)
 
 
 def measured_peaks() -> dict:
@@ -193,6 +220,111 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_batched(dev) -> dict:
+    import torch
+
+    from apsep_gb300 import Plan
+    from apsep_gb300.workloads import batch_workload
+
+    S = 4096
+    x, offs = batch_workload(S, seed=7, device=dev)
+    n = x.numel()
+    d_off = torch.from_numpy(offs).to(dev)
+    out = torch.empty(n, dtype=torch.int32, device=dev)
+    plan = Plan(n, torch.int32, device=dev)
+    useful = 8.0 * n + 8.0 * (S + 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        plan.run_segmented(x, d_off, out=out)
+    plan.check()
+    ts = []
+    for _ in range(7):
+        e0.record()
+        plan.run_segmented(x, d_off, out=out)
+        e1.record()
+        plan.check()
+        ts.append(e0.elapsed_time(e1))
+    batched_ms = statistics.median(ts)
+    bounds = [(int(offs[i]), int(offs[i + 1])) for i in range(S)]
+    loop_ts = []
+    for _ in range(2):
+        torch.cuda.synchronize(dev)
+        e0.record()
+        for a, b in bounds:
+            if b > a:
+                plan.run(x[a:b], out=out[a:b])
+        e1.record()
+        plan.check()
+        loop_ts.append(e0.elapsed_time(e1))
+    loop_ms = min(loop_ts)
+    plan.close()
+    return {"workload": "batch_4096_loguniform_32_2p20_int32", "segments": S, "keys": n,
+            "useful_bytes": int(useful), "batched_ms": round(batched_ms, 4), "loop_ms": round(loop_ms, 3),
+            "batched_gbs": round(useful / batched_ms / 1e6, 1), "loop_gbs": round(useful / loop_ms / 1e6, 2),
+            "speedup_vs_loop": round(loop_ms / batched_ms, 2), "launches": {"batched": 1, "loop": S},
+            "note": "device time (CUDA events); the loop is enqueued from Python, one apsep_run per array"}
+
+
+def run_served(dev) -> dict:
+    from apsep_gb300.serve import Server, plain_loop
+    from apsep_gb300.workloads import serve_requests
+
+    server = Server(budget_bytes=8 << 30, slot_keys=48 << 20, device=dev)
+    try:
+        server.serve(serve_requests(32, rate=0.0, seed=3), realtime=False)  # warm-up
+        sat = server.serve(serve_requests(400, rate=0.0, seed=21), realtime=False)
+        base = plain_loop(serve_requests(400, rate=0.0, seed=21), realtime=False, device=dev)
+        rate = 0.5 * sat.requests_per_s
+        live = server.serve(serve_requests(400, rate=rate, seed=22), realtime=True)
+    finally:
+        server.close()
+    return {"workload": "serve_loguniform_2p10_2p24_i32_f32", "budget_bytes": 8 << 30,
+            "pool_bytes": sat.device_bytes, "saturated": sat.as_dict(), "plain_loop_saturated": base.as_dict(),
+            "throughput_vs_plain_loop": round(sat.requests_per_s / base.requests_per_s, 2),
+            "offered_load_req_per_s": round(rate, 1), "at_offered_load": live.as_dict(),
+            "note": "wall clock on the host; every request copies its keys in and its answers out"}
+
+
+def run_sweep(dev, peak_gbs: float) -> list:
+    import torch
+
+    from apsep_gb300 import Plan
+
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    rows = []
+    nmax = 1 << 30
+    plan = Plan(nmax, torch.int32, device=dev)
+    out = torch.empty(nmax, dtype=torch.int32, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for lg in range(14, 31, 2):
+        n = 1 << lg
+        for name in ("uniform", "descending"):
+            if name == "uniform":
+                x = torch.randint(0, 1 << 31, (n,), generator=g, device=dev, dtype=torch.int64).to(torch.int32)
+            else:
+                x = torch.arange(n - 1, -1, -1, device=dev, dtype=torch.int32)
+            for _ in range(3):
+                plan.run(x, out=out[:n])
+            ts = []
+            for _ in range(5 if lg < 28 else 3):
+                flush.zero_()
+                e0.record()
+                plan.run(x, out=out[:n])
+                e1.record()
+                plan.check()
+                ts.append(e0.elapsed_time(e1))
+            ms = statistics.median(ts)
+            gbs = useful_gbs(n, ms / 1e3)
+            rows.append({"log2_n": lg, "dist": name, "us": round(ms * 1e3, 2), "gbs": round(gbs, 1),
+                         "frac": round(gbs / peak_gbs, 4)})
+            del x
+    plan.close()
+    del out
+    return rows
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -266,10 +398,7 @@ def run_ours(args) -> None:
     plan.check()
     e2e_ms = sum(a.elapsed_time(b) for a, b in ev2)
 
-    t = torch.tensor([total_ms, e2e_ms], dtype=torch.float64, device=dev)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms, e2e_ms = float(t[0]), float(t[1])
+    total_ms, e2e_ms = max_over_ranks([total_ms, e2e_ms], dist, dev)
     clocks = {}
     if rank == 0:
         sampler.mark(t_wall0, t_wall1)
@@ -280,7 +409,7 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
         return
 
-    value = useful_gbs(N, total_ms / 1e3, args.steps * world)
+    value = whole_job_gbs(N, total_ms, args.steps, world)
     per = {}
     for j, name in enumerate(DISTS):
         ms = [step_ms[i] for i in range(args.steps) if i % 4 == j]
@@ -307,7 +436,7 @@ def run_ours(args) -> None:
                      "algorithmic_bytes_per_launch": 8 * N,
                      "traffic": traffic.get("bytes_per_launch") if traffic else None,
                      "traffic_source": traffic.get("source") if traffic else None},
-        "e2e": {"value": round(useful_gbs(N, e2e_ms / 1e3, args.steps * world), 2), "unit": UNIT,
+        "e2e": {"value": round(whole_job_gbs(N, e2e_ms, args.steps, world), 2), "unit": UNIT,
                 "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
         "gpu_launches": args.steps,
         "clocks": clocks,
@@ -315,8 +444,18 @@ def run_ours(args) -> None:
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(host)
+    if world == 1 and not args.no_extras:
+        plan.close()
+        del d_in, out, flush
+        torch.cuda.empty_cache()
+        line["batched"] = run_batched(dev)
+        torch.cuda.empty_cache()
+        line["served"] = run_served(dev)
+        torch.cuda.empty_cache()
+        line["sweep"] = run_sweep(dev, peaks["hbm_gbs"])
     print(json.dumps(line), flush=True)
-    plan.close()
+    if world > 1 or args.no_extras:
+        plan.close()
     if dist:
         dist.destroy_process_group()
 
@@ -328,6 +467,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched / served / sweep objects")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
