@@ -551,11 +551,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
 
             // ---- 2. warp prefix minima over lane minima ---------------------------------
-            T pre = lmin;
+            T pre = lmin, suf = lmin;  // inclusive prefix / suffix minima over lanes, side by side
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const T nb = __shfl_up_sync(FULL, pre, o);
+                const T na = __shfl_down_sync(FULL, suf, o);
                 if (lane >= o) pre = KeyTraits<T>::vmin(pre, nb);
+                if (lane + o < 32) suf = KeyTraits<T>::vmin(suf, na);
             }
             const T before = __shfl_up_sync(FULL, pre, 1);  // min of the lanes before (lane > 0)
             const T tile_min_t = __shfl_sync(FULL, pre, 31);
@@ -675,43 +677,81 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             const bool wvalid = widx < stk_hi;
             const T wv = wvalid ? sStkV[widx & (K - 1)] : KeyTraits<T>::pad();
             unsigned cm = 0;
-            {
-                const int smax = (int)__reduce_max_sync(FULL, (unsigned)__popc(sm));
-                if (smax) {
-                    const int wcnt = stk_hi - win_lo;  // window entries (uniform)
-                    const int wp = wvalid ? sStkP[widx & (K - 1)] : -1;
+            if (__any_sync(FULL, sm != 0)) {
+                const int wcnt = stk_hi - win_lo;  // window entries (uniform)
+                const int wp = wvalid ? sStkP[widx & (K - 1)] : -1;
+                // the answer of q: the topmost qualifying window entry (by a 6-step
+                // shuffle search), else a binary search below the window; -1 = miss
+                auto search = [&](T q, bool act) {
+                    int lo = -1;
+#pragma unroll
+                    for (int s2 = 32; s2 > 0; s2 >>= 1) {
+                        const int cand = lo + s2;
+                        const T wc = __shfl_sync(FULL, wv, cand & 31);
+                        if (act && cand < wcnt && lt<INCL>(wc, q)) lo = cand;
+                    }
+                    const int ap = __shfl_sync(FULL, wp, lo & 31);
+                    int ans = -1;
+                    if (act) {
+                        ans = lo >= 0 ? ap : -1;
+                        if (lo < 0 && win_lo > stk_lo) {
+                            int l2 = stk_lo, h2 = win_lo;
+                            while (l2 < h2) {
+                                const int mid = (l2 + h2) >> 1;
+                                if (lt<INCL>(sStkV[mid & (K - 1)], q)) l2 = mid + 1;
+                                else h2 = mid;
+                            }
+                            if (l2 > stk_lo) ans = sStkP[(l2 - 1) & (K - 1)];
+                        }
+                    }
+                    return ans;
+                };
+                const int cs = __popc(sm);
+                int stot;
+                const int soff = warp_excl_sum(cs, stot);
+                const int smax = (int)__reduce_max_sync(FULL, (unsigned)cs);
+                if (smax > 1 && stot <= 32) {
+                    // The tile's S keys sit mostly in its first lanes: spread them, one per
+                    // lane, over a single round (the X list is consumed, its space is free).
+                    __syncwarp();
+                    {
+                        int o = soff;
+                        unsigned m = sm;
+                        while (m) {
+                            const int k = __ffs(m) - 1;
+                            m &= m - 1;
+                            sList[o++] = (int16_t)(lane * IPT + k);
+                        }
+                    }
+                    __syncwarp();
+                    const bool act = lane < stot;
+                    const int e = act ? (int)sList[lane] : 0;
+                    const int ans = search(act ? V[swz(e)] : KeyTraits<T>::pad(), act);
+                    if (act) O[swz(e)] = ans >= 0 ? ans : -2;  // -2: a miss, flagged by the key's lane
+                    __syncwarp();
+                    unsigned m = sm;
+                    while (m) {
+                        const int k = __ffs(m) - 1;
+                        m &= m - 1;
+                        if (O[swz(lane * IPT + k)] == -2) {
+                            O[swz(lane * IPT + k)] = -1;
+                            cm |= 1u << k;
+                        }
+                    }
+                } else {
                     unsigned m = sm;
                     for (int rd = 0; rd < smax; rd++) {
                         const bool act = m != 0;
                         const int k = act ? __ffs(m) - 1 : 0;
                         m &= m - 1;
-                        const T q = act ? V[swz(lane * IPT + k)] : KeyTraits<T>::pad();
-                        // topmost window entry that qualifies (they form a bottom part)
-                        int lo = -1;
-#pragma unroll
-                        for (int s2 = 32; s2 > 0; s2 >>= 1) {
-                            const int cand = lo + s2;
-                            const T wc = __shfl_sync(FULL, wv, cand & 31);
-                            if (act && cand < wcnt && lt<INCL>(wc, q)) lo = cand;
-                        }
-                        const int ap = __shfl_sync(FULL, wp, lo & 31);
+                        const int ans = search(act ? V[swz(lane * IPT + k)] : KeyTraits<T>::pad(), act);
                         if (act) {
-                            int ans = lo >= 0 ? ap : -1;
-                            if (lo < 0 && win_lo > stk_lo) {  // below the window: binary search
-                                int l2 = stk_lo, h2 = win_lo;
-                                while (l2 < h2) {
-                                    const int mid = (l2 + h2) >> 1;
-                                    if (lt<INCL>(sStkV[mid & (K - 1)], q)) l2 = mid + 1;
-                                    else h2 = mid;
-                                }
-                                if (l2 > stk_lo) ans = sStkP[(l2 - 1) & (K - 1)];
-                            }
                             if (ans >= 0) O[swz(lane * IPT + k)] = ans;
                             else cm |= 1u << k;
                         }
                     }
-                    if (cm && !dropped) atomicOr(err, ERR_INTERNAL);
                 }
+                if (cm && !dropped) atomicOr(err, ERR_INTERNAL);
             }
 
             // ---- 6. flagged keys: deferred (D) and capped (C) -----------------------------
@@ -792,12 +832,6 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 
             // ---- 8. stack update: pop what the tile dominates, push its suffix minima ----
             {
-                T suf = lmin;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const T nb = __shfl_down_sync(FULL, suf, o);
-                    if (lane + o < 32) suf = KeyTraits<T>::vmin(suf, nb);
-                }
                 const T after_w = __shfl_down_sync(FULL, suf, 1);  // min of the lanes after (lane < 31)
                 unsigned fmask = 0;
                 const bool has_aft = lane < 31;
