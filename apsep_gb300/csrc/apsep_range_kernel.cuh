@@ -490,6 +490,63 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             const int lb = tile_base + lane * IPT;  // position of this lane's first key
             const int nvalid = min(max(a.n - lb, 0), IPT);
+
+            // ---- a whole tile below the range so far --------------------------------------
+            // A tile that never increases (under the comparator, lane boundaries
+            // included) and whose first key has no qualifying key earlier in the
+            // range has no answer for any key inside the range: every key is deferred,
+            // every stack entry (>= the range minimum >= the first key) is popped and
+            // the tile's last key is its only strict suffix minimum.  (Single arrays.)
+            if constexpr (!SEG) {
+                bool dec = valid_keys == WT;
+#pragma unroll
+                for (int k = 1; k < IPT; k++) dec = dec && !lt<INCL>(v[k - 1], v[k]);
+                const T prev_last = __shfl_up_sync(FULL, v[IPT - 1], 1);
+                dec = dec && (lane == 0 || !lt<INCL>(prev_last, v[0]));
+                const T first = __shfl_sync(FULL, v[0], 0);
+                if (__all_sync(FULL, dec) && (!has_rmin || !lt<INCL>(rmin, first))) {
+                    const int4 m1 = make_int4(-1, -1, -1, -1);
+#pragma unroll
+                    for (int q4 = 0; q4 < IPT / 4; q4++) *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) = m1;
+                    if (((lane + 1) & (TPC - 1)) == 0) __stcg(&chunk_min_w[(size_t)t * W + lane / TPC], v[IPT - 1]);
+                    const T tmin = __shfl_sync(FULL, v[IPT - 1], 31);
+                    for (int e = lane; e < WT && def_total + e < kDefCap; e += 32) {
+                        sDefP[def_total + e] = tile_base + e;
+                        sDefV[def_total + e] = V[swz(e)];
+                    }
+                    if (lane < W) __stcg(&a.s.tile_mask[(size_t)t * MW + lane], 0xffffffffu);
+                    if (lane == 0) {
+                        __stcg(&a.s.tile_flag[t], (uint32_t)WT);
+                        __stcg(&tile_min_w[t], tmin);
+                    }
+                    def_total += WT;
+                    fence_proxy_async_smem();
+                    __syncwarp();
+                    if (full) {
+                        if (lane == 0) {
+                            tma_store_2d(&map_out, 0, t * W, O);
+                            bulk_commit();
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < IPT; j++) a.d_out[tile_base + j * 32 + lane] = -1;
+                    }
+                    if (lane == 31) {
+                        sStkV[stk_lo & (K - 1)] = v[IPT - 1];
+                        sStkP[stk_lo & (K - 1)] = tile_base + WT - 1;
+                    }
+                    stk_hi = stk_lo + 1;
+                    rmin = tmin;
+                    has_rmin = true;
+                    __syncwarp();
+                    if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
+                        mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * 4));
+                        tma_load_2d(V, &map_in, 0, (t + kStages) * W, &bar[slot]);
+                    }
+                    continue;
+                }
+            }
+
             unsigned umask = 0;     // keys without an in-thread answer
             bool all_inc = false;   // the whole tile increases: every key answers its predecessor
             {
