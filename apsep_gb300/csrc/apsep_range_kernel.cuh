@@ -490,6 +490,18 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             const int lb = tile_base + lane * IPT;  // position of this lane's first key
             const int nvalid = min(max(a.n - lb, 0), IPT);
+            // Monotone lanes: each key answers its neighbour (adj), or no key answers
+            // any later one (none); across the lane boundary likewise (b_adj, b_none).
+            bool adj = true, none = true;
+#pragma unroll
+            for (int k = 1; k < IPT; k++) {
+                const bool l = lt<INCL>(v[k - 1], v[k]);
+                adj = adj && l;
+                none = none && !l;
+            }
+            const unsigned mono = __ballot_sync(FULL, adj || none);
+            const T prev_last = __shfl_up_sync(FULL, v[IPT - 1], 1);
+            const bool b_adj = lane == 0 || lt<INCL>(prev_last, v[0]);
 
             // ---- a whole tile below the range so far --------------------------------------
             // A tile that never increases (under the comparator, lane boundaries
@@ -498,13 +510,9 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             // every stack entry (>= the range minimum >= the first key) is popped and
             // the tile's last key is its only strict suffix minimum.  (Single arrays.)
             if constexpr (!SEG) {
-                bool dec = valid_keys == WT;
-#pragma unroll
-                for (int k = 1; k < IPT; k++) dec = dec && !lt<INCL>(v[k - 1], v[k]);
-                const T prev_last = __shfl_up_sync(FULL, v[IPT - 1], 1);
-                dec = dec && (lane == 0 || !lt<INCL>(prev_last, v[0]));
                 const T first = __shfl_sync(FULL, v[0], 0);
-                if (__all_sync(FULL, dec) && (!has_rmin || !lt<INCL>(rmin, first))) {
+                if (mono == FULL && valid_keys == WT && __all_sync(FULL, none && (lane == 0 || !b_adj)) &&
+                    (!has_rmin || !lt<INCL>(rmin, first))) {
                     const int4 m1 = make_int4(-1, -1, -1, -1);
 #pragma unroll
                     for (int q4 = 0; q4 < IPT / 4; q4++) *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) = m1;
@@ -547,26 +555,68 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 }
             }
 
+            // ---- a whole tile above the stack top (strict comparator) -----------------------
+            // A strictly increasing tile whose first key is above the stack's top entry
+            // (the range's last key): every key answers its predecessor, every key is a
+            // strict suffix minimum, and the ring keeps the tile's last K keys.
+            if constexpr (!SEG && !INCL) {  // (strict comparator: adj means strictly increasing)
+                const T first = __shfl_sync(FULL, v[0], 0);
+                if (mono == FULL && valid_keys == WT && __all_sync(FULL, adj && b_adj) && stk_hi > stk_lo &&
+                    sStkV[(stk_hi - 1) & (K - 1)] < first) {
+                    const int top_pos = sStkP[(stk_hi - 1) & (K - 1)];
+#pragma unroll
+                    for (int q4 = 0; q4 < IPT / 4; q4++)
+                        *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) =
+                            make_int4(lane == 0 && q4 == 0 ? top_pos : lb + 4 * q4 - 1, lb + 4 * q4, lb + 4 * q4 + 1,
+                                      lb + 4 * q4 + 2);
+                    if ((lane & (TPC - 1)) == 0) __stcg(&chunk_min_w[(size_t)t * W + lane / TPC], v[0]);
+                    if (lane == 0) {
+                        __stcg(&a.s.tile_flag[t], 0u);
+                        __stcg(&tile_min_w[t], first);
+                    }
+                    fence_proxy_async_smem();
+                    __syncwarp();
+                    if (full) {
+                        if (lane == 0) {
+                            tma_store_2d(&map_out, 0, t * W, O);
+                            bulk_commit();
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < IPT; j++) a.d_out[tile_base + j * 32 + lane] = O[swz(j * 32 + lane)];
+                    }
+                    const int base_idx = stk_hi;  // entry of tile key e: base_idx + e
+                    if (lane * IPT >= WT - K) {
+#pragma unroll
+                        for (int k = 0; k < IPT; k++) {
+                            sStkV[(base_idx + lane * IPT + k) & (K - 1)] = v[k];
+                            sStkP[(base_idx + lane * IPT + k) & (K - 1)] = lb + k;
+                        }
+                    }
+                    stk_hi = base_idx + WT;
+                    stk_lo = stk_hi - K;
+                    dropped = true;  // WT > K: the older entries are gone
+                    rmin = KeyTraits<T>::vmin(rmin, first);
+                    __syncwarp();
+                    if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
+                        mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * 4));
+                        tma_load_2d(V, &map_in, 0, (t + kStages) * W, &bar[slot]);
+                    }
+                    continue;
+                }
+            }
+
             unsigned umask = 0;     // keys without an in-thread answer
             bool all_inc = false;   // the whole tile increases: every key answers its predecessor
             {
                 int res[IPT];  // absolute answers, -1 = none in the thread
                 res[0] = -1;
-                // Monotone lanes (each key answers its neighbour, or no key answers any
-                // later one) need no ladder.
-                bool adj = true, none = true;
-#pragma unroll
-                for (int k = 1; k < IPT; k++) {
-                    const bool l = lt<INCL>(v[k - 1], v[k]);
-                    adj = adj && l;
-                    none = none && !l;
-                }
-                if (__all_sync(FULL, adj || none)) {
+                // Monotone lanes need no ladder.
+                if (mono == FULL) {
 #pragma unroll
                     for (int k = 1; k < IPT; k++) res[k] = adj ? lb + k - 1 : -1;
                     // every key answers its predecessor across lane boundaries too
-                    const T prev_last = __shfl_up_sync(FULL, v[IPT - 1], 1);
-                    all_inc = __all_sync(FULL, adj && (lane == 0 || lt<INCL>(prev_last, v[0]))) && valid_keys == WT;
+                    all_inc = __all_sync(FULL, adj && b_adj) && valid_keys == WT;
                     if (all_inc && lane > 0) res[0] = lb - 1;
                 } else {
 #pragma unroll
