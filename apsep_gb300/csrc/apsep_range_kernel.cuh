@@ -71,7 +71,7 @@ struct WLayout {
 };
 
 template <int IPT, int WPC>
-constexpr size_t kernel_smem_bytes() { return WLayout<IPT>::kBytes * WPC + 1024; }
+constexpr size_t kernel_smem_bytes() { return WLayout<IPT>::kBytes * WPC + 1024 + 64; }  // + CTA words
 
 __device__ __forceinline__ uint32_t make_tag(uint32_t epoch, uint32_t flag) { return (epoch << 2) | flag; }
 
@@ -346,8 +346,10 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    unsigned char* wsm =
-        (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023) + (size_t)warp * L::kBytes;
+    unsigned char* cta_sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* wsm = cta_sm + (size_t)warp * L::kBytes;
+    // CTA words: [0] the CTA's first range, [1] warps of the CTA finished
+    int* sCta = (int*)(cta_sm + (size_t)WPC * L::kBytes);
     T* sV = (T*)(wsm + L::kV);
     int32_t* O = (int32_t*)(wsm + L::kO);
     T* sSM = (T*)(wsm + L::kSM);
@@ -365,16 +367,21 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     T* chunk_min_w = (T*)a.s.chunk_min;
     uint32_t* err = &a.s.ctr->err;
 
-    int r = 0;
+    // One claim per CTA: its warps take WPC consecutive range ids, in the order
+    // the CTAs start (so every range a warp may wait on belongs to a started CTA).
+    if (threadIdx.x == 0) {
+        sCta[0] = (int)atomicAdd(&a.s.ctr->range_counter, (unsigned)WPC);
+        sCta[1] = 0;
+    }
     uint32_t epoch = 0;
     if (lane == 0) {
-        r = (int)atomicAdd(&a.s.ctr->range_counter, 1u);
         epoch = ld_relaxed_u32(&a.s.ctr->epoch);
         for (int s = 0; s < kStages; s++) mbar_init(&bar[s], 1);
         fence_mbarrier_init();
         fence_proxy_async_smem();
     }
-    r = __shfl_sync(FULL, r, 0);
+    __syncthreads();  // the CTA's claim is in shared memory
+    const int r = sCta[0] + warp;
     epoch = __shfl_sync(FULL, epoch, 0);
     __syncwarp();
 
@@ -1191,12 +1198,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     }
 
     // ---- run bookkeeping: the last warp resets the control block --------------------------
+    // (the last warp of each CTA counts the CTA in; the last CTA resets)
     __syncwarp();
     int last = 0;
-    if (lane == 0) {
+    if (lane == 0 && atomicAdd(&sCta[1], 1) == WPC - 1) {
         __threadfence();
         const uint32_t prev = atomicAdd(&a.s.ctr->done, 1u);
-        last = prev == gridDim.x * WPC - 1;
+        last = prev == gridDim.x - 1;
         if (last) {
             a.s.ctr->range_counter = 0;
             a.s.ctr->done = 0;
