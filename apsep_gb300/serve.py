@@ -21,6 +21,13 @@ is completion minus arrival on the server clock.
 
 `plain_loop` is the baseline the server is measured against: one request at
 a time, copy in, apsep_run, copy out, synchronise.
+
+Device-resident requests (`ResidentServer`): when the keys are produced on
+the GPU (or uploaded by the client ahead of time), the pool is a ring of
+keys and answers in HBM that requests occupy in arrival order.  A batch is a
+contiguous span of arrived requests and runs in place, one segmented launch
+with no copies; `resident_loop` is its per-request baseline (one apsep_run
+per request on the same memory, synchronised).
 """
 from __future__ import annotations
 
@@ -270,5 +277,130 @@ def plain_loop(requests: list, keep_answers: bool = False, realtime: bool = True
     for p in plans.values():
         p.check()
         p.close()
+    lat = [1e3 * (r.t_done - (r.arrival if realtime else 0.0)) for r in order]
+    return ServeStats(len(order), sum(r.n for r in order), t_end, lat, len(order), 0)
+
+
+# ---------------------------------------------------------------------------
+# Device-resident requests
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class ResidentRequest:
+    rid: int
+    start: int            # first key in the ring
+    n: int
+    arrival: float = 0.0
+    t_done: float | None = None
+
+
+class ResidentServer:
+    """Requests whose keys already sit in a device ring (in arrival order).
+
+    keys/answers: the ring (device tensors of equal length); requests must
+    not wrap.  Each batch is the longest run of arrived, waiting requests
+    that fits `max_batch_keys` and `max_segments`, launched in place."""
+
+    def __init__(self, keys: torch.Tensor, answers: torch.Tensor, inclusive: bool = False,
+                 max_batch_keys: int = 64 << 20, max_segments: int = 4096, streams: int = 2,
+                 budget_bytes: int = 8 << 30):
+        self.keys, self.answers = keys, answers
+        self.device = keys.device
+        self.max_batch_keys = int(min(max_batch_keys, keys.numel()))
+        self.max_segments = int(max_segments)
+        # the ring plus each lane's plan must fit the HBM budget
+        need = keys.numel() * 8 + streams * (self.max_batch_keys * (slot_bytes_per_key() - 8.0) +
+                                             8 * (max_segments + 1))
+        if need > budget_bytes:
+            raise ValueError("ring and plans need %d bytes, over the budget of %d" % (need, budget_bytes))
+        self.device_bytes = int(need)
+        self.lanes = []
+        for _ in range(streams):
+            self.lanes.append({"stream": torch.cuda.Stream(device=self.device), "event": torch.cuda.Event(),
+                               "offs": torch.empty(max_segments + 1, dtype=torch.int64, device=self.device),
+                               "offs_host": torch.empty(max_segments + 1, dtype=torch.int64).pin_memory(),
+                               "plan": Plan(min(int(max_batch_keys), keys.numel()), keys.dtype,
+                                            inclusive=inclusive, device=self.device),
+                               "batch": []})
+
+    def close(self):
+        for ln in self.lanes:
+            ln["plan"].close()
+
+    def _launch(self, ln, batch):
+        base = batch[0].start
+        offs = [0]
+        for r in batch:
+            offs.append(offs[-1] + r.n)
+        total = offs[-1]
+        ns = len(batch)
+        ln["batch"] = batch
+        with torch.cuda.stream(ln["stream"]):
+            ln["offs_host"][:ns + 1] = torch.tensor(offs, dtype=torch.int64)
+            ln["offs"][:ns + 1].copy_(ln["offs_host"][:ns + 1], non_blocking=True)
+            ln["plan"].run_segmented(self.keys[base:base + total], ln["offs"][:ns + 1],
+                                     out=self.answers[base:base + total], stream=ln["stream"])
+            ln["event"].record(ln["stream"])
+
+    def serve(self, requests: list, realtime: bool = True) -> ServeStats:
+        order = sorted(requests, key=lambda r: r.start)
+        for a, b in zip(order, order[1:]):
+            if b.start != a.start + a.n:
+                raise ValueError("resident requests must lie back to back in the ring, in arrival order")
+        nxt = done = batches = 0
+        waiting = collections.deque()
+        torch.cuda.synchronize(self.device)
+        t0 = time.perf_counter()
+        while done < len(order):
+            now = time.perf_counter() - t0
+            while nxt < len(order) and (not realtime or order[nxt].arrival <= now):
+                waiting.append(order[nxt])
+                nxt += 1
+            progressed = False
+            for ln in self.lanes:
+                if ln["batch"] and ln["event"].query():
+                    t = time.perf_counter() - t0
+                    for r in ln["batch"]:
+                        r.t_done = t
+                    done += len(ln["batch"])
+                    ln["batch"] = []
+                    progressed = True
+                if not ln["batch"] and waiting:
+                    batch, keys = [], 0
+                    while (waiting and len(batch) < self.max_segments and
+                           (not batch or keys + waiting[0].n <= self.max_batch_keys)):
+                        r = waiting.popleft()
+                        batch.append(r)
+                        keys += r.n
+                    self._launch(ln, batch)
+                    batches += 1
+                    progressed = True
+            if not progressed:
+                time.sleep(0)
+        t_end = time.perf_counter() - t0
+        for ln in self.lanes:
+            ln["plan"].check(stream=ln["stream"])
+        lat = [1e3 * (r.t_done - (r.arrival if realtime else 0.0)) for r in order]
+        return ServeStats(len(order), sum(r.n for r in order), t_end, lat, batches, self.device_bytes)
+
+
+def resident_loop(keys: torch.Tensor, answers: torch.Tensor, requests: list, inclusive: bool = False,
+                  realtime: bool = True) -> ServeStats:
+    """The per-request baseline on device-resident keys: apsep_run, synchronise."""
+    nmax = max(r.n for r in requests)
+    plan = Plan(nmax, keys.dtype, inclusive=inclusive, device=keys.device)
+    stream = torch.cuda.current_stream(keys.device)
+    order = sorted(requests, key=lambda r: r.arrival if realtime else 0.0)
+    torch.cuda.synchronize(keys.device)
+    t0 = time.perf_counter()
+    for r in order:
+        if realtime:
+            while time.perf_counter() - t0 < r.arrival:
+                pass
+        plan.run(keys[r.start:r.start + r.n], out=answers[r.start:r.start + r.n])
+        stream.synchronize()
+        r.t_done = time.perf_counter() - t0
+    t_end = time.perf_counter() - t0
+    plan.check()
+    plan.close()
     lat = [1e3 * (r.t_done - (r.arrival if realtime else 0.0)) for r in order]
     return ServeStats(len(order), sum(r.n for r in order), t_end, lat, len(order), 0)

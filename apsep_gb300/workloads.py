@@ -78,3 +78,30 @@ def serve_requests(count: int, rate: float, seed: int = 11, lo: int = 1 << 10, h
         pool = pool_i if rng.random() < 0.5 else pool_f
         reqs.append(Request(rid=i, keys=pool[start:start + L], arrival=float(arrivals[i])))
     return reqs
+
+
+def resident_requests(count: int, rate: float, seed: int = 11, lo: int = 1 << 10, hi: int = 1 << 24,
+                      dtype=torch.int32, device="cuda"):
+    """The served workload's lengths and arrivals, keys generated in place in a
+    device ring (back to back, arrival order).  Returns (keys, answers, requests)."""
+    from .serve import ResidentRequest
+
+    rng = np.random.default_rng(seed)
+    lengths = segment_lengths(count, lo, hi, seed + 1)
+    gaps = rng.exponential(1.0 / rate, count) if rate > 0 else np.zeros(count)
+    arrivals = np.cumsum(gaps)
+    n = int(lengths.sum())
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    if dtype == torch.int32:
+        keys = torch.randint(0, 1 << 31, (n,), generator=g, device=device, dtype=torch.int64).to(torch.int32)
+    else:
+        u = torch.randint(0, 1 << 24, (n,), generator=g, device=device, dtype=torch.int64)
+        keys = (-1e6 + u.to(torch.float64) * (2e6 / (1 << 24))).to(torch.float32)
+    answers = torch.empty(n, dtype=torch.int32, device=device)
+    reqs, pos = [], 0
+    for i in range(count):
+        L = int(lengths[i])
+        reqs.append(ResidentRequest(rid=i, start=pos, n=L, arrival=float(arrivals[i])))
+        pos += L
+    return keys, answers, reqs

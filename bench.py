@@ -36,7 +36,8 @@ Extra objects on the same line (one GPU only; --no-extras skips them):
              answers out through device-resident pools within an 8 GiB HBM
              budget.  Saturated throughput against the plain per-request loop,
              then p50/p99 latency at a Poisson offered load of half the
-             server's saturated rate.
+             server's saturated rate.  served.resident: the same stream with
+             the keys already in a device ring (batches run in place).
   sweep      single-array useful GB/s and roofline fraction for N = 2^14 ..
              2^30 (every second power of two), uniform and descending keys.
 
@@ -278,11 +279,44 @@ def run_served(dev) -> dict:
         live = server.serve(serve_requests(400, rate=rate, seed=22), realtime=True)
     finally:
         server.close()
-    return {"workload": "serve_loguniform_2p10_2p24_i32_f32", "budget_bytes": 8 << 30,
+    resident = run_served_resident(dev)
+    return {"workload": "serve_loguniform_2p10_2p24_i32_f32", "budget_bytes": 8 << 30, "resident": resident,
             "pool_bytes": sat.device_bytes, "saturated": sat.as_dict(), "plain_loop_saturated": base.as_dict(),
             "throughput_vs_plain_loop": round(sat.requests_per_s / base.requests_per_s, 2),
             "offered_load_req_per_s": round(rate, 1), "at_offered_load": live.as_dict(),
             "note": "wall clock on the host; every request copies its keys in and its answers out"}
+
+
+def run_served_resident(dev) -> dict:
+    """The same request stream with keys already in a device ring (int32)."""
+    import torch
+
+    from apsep_gb300.serve import ResidentServer, resident_loop
+    from apsep_gb300.workloads import resident_requests
+
+    keys, answers, reqs = resident_requests(400, rate=0.0, seed=23, device=dev)
+    srv = ResidentServer(keys, answers, max_batch_keys=160 << 20)
+    try:
+        srv.serve(reqs[:32], realtime=False)  # warm-up
+        sat = srv.serve(reqs, realtime=False)
+        base = resident_loop(keys, answers, reqs, realtime=False)
+        rate = 0.5 * sat.requests_per_s
+        keys2, answers2, reqs2 = resident_requests(400, rate=rate, seed=24, device=dev)
+        srv2 = ResidentServer(keys2, answers2, max_batch_keys=160 << 20)
+        try:
+            live = srv2.serve(reqs2, realtime=True)
+        finally:
+            srv2.close()
+    finally:
+        srv.close()
+    del keys, answers
+    torch.cuda.empty_cache()
+    return {"workload": "serve_resident_loguniform_2p10_2p24_i32", "budget_bytes": 8 << 30,
+            "pool_bytes": sat.device_bytes,
+            "saturated": sat.as_dict(), "plain_loop_saturated": base.as_dict(),
+            "throughput_vs_plain_loop": round(sat.requests_per_s / base.requests_per_s, 2),
+            "offered_load_req_per_s": round(rate, 1), "at_offered_load": live.as_dict(),
+            "note": "keys produced in place in a device ring; batches run in place, no copies"}
 
 
 def run_sweep(dev, peak_gbs: float) -> list:

@@ -6,8 +6,8 @@ import torch
 
 import oracle
 from apsep_gb300 import Plan, autotune
-from apsep_gb300.serve import Server, plain_loop
-from apsep_gb300.workloads import serve_requests
+from apsep_gb300.serve import ResidentServer, Server, plain_loop, resident_loop
+from apsep_gb300.workloads import resident_requests, serve_requests
 
 pytestmark = pytest.mark.gpu
 
@@ -68,3 +68,21 @@ def test_autotune_table_and_tuned_plan():
             out = p.run(torch.from_numpy(a).cuda())
             p.check()
             assert np.array_equal(out.cpu().numpy(), oracle.apse(a))
+
+
+@pytest.mark.parametrize("dtype", [torch.int32, torch.float32])
+def test_resident_server_matches_oracle_and_loop(dtype):
+    keys, answers, reqs = resident_requests(120, rate=0.0, seed=9, hi=1 << 18, dtype=dtype)
+    srv = ResidentServer(keys, answers, max_batch_keys=1 << 20, max_segments=64)
+    try:
+        st = srv.serve(reqs, realtime=False)
+    finally:
+        srv.close()
+    assert st.requests == 120 and st.batches < 120
+    got = answers.cpu().numpy()
+    k = keys.cpu().numpy()
+    for r in reqs[::7]:  # a sample of the requests, each checked in full
+        assert np.array_equal(got[r.start:r.start + r.n], oracle.apse(k[r.start:r.start + r.n])), r.rid
+    answers.fill_(-7)
+    resident_loop(keys, answers, reqs, realtime=False)
+    assert np.array_equal(answers.cpu().numpy(), got)
