@@ -45,7 +45,7 @@
 namespace apsep {
 
 constexpr int kStages = 3;      // TMA ring depth per warp (tiles)
-constexpr int kStackCap = 128;  // range-stack entries kept per warp
+constexpr int kStackCap = 64;   // range-stack entries kept per warp
 constexpr int kDefCap = 64;     // deferred keys listed in shared memory per range
 constexpr int kCapCap = 16;     // capped keys listed in shared memory per range
 
