@@ -30,6 +30,7 @@ struct apsep_plan {
 namespace {
 
 constexpr uint32_t kDefaultSpinLimit = 1u << 22;  // ~1 s of polling with back-off
+constexpr int64_t kMaxKeysPerRun = (int64_t)INT32_MAX - 4095;  // APSEP_MAX_KEYS
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
@@ -117,7 +118,9 @@ apsep_status apsep_plan_create(apsep_plan** out, apsep_dtype dtype, apsep_cmp cm
     *out = nullptr;
     if ((dtype != APSEP_INT32 && dtype != APSEP_FLOAT32) || (cmp != APSEP_LT && cmp != APSEP_LE))
         return APSEP_EINVAL;
-    if (capacity < 0 || capacity > (int64_t)INT32_MAX) return APSEP_EINVAL;
+    // int32 positions; the last tile's end (up to n rounded up to whole tiles)
+    // must stay below 2^31 as well
+    if (capacity < 0 || capacity > kMaxKeysPerRun) return APSEP_EINVAL;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return APSEP_ECUDA;
     int major = 0;

@@ -4,7 +4,7 @@
  * All Previous Smaller Element: for each key a[i], out[i] is the largest
  * j < i with a[j] < a[i] (APSEP_LT) or a[j] <= a[i] (APSEP_LE), else -1.
  * Keys are int32 or float32 (finite: NaN keys are outside the contract),
- * outputs are int32 indices, so n < 2^31.
+ * outputs are int32 indices, so n <= APSEP_MAX_KEYS = 2^31 - 4096.
  *
  * Plain pointers and sizes only: device pointers from any allocator
  * (cudaMalloc, torch), `stream` is a cudaStream_t passed as void* (NULL = the
@@ -122,6 +122,9 @@ apsep_status apsep_config_shape(int32_t config, int32_t* threads, int32_t* keys_
 /* One-shot: plan, run on the legacy default stream, synchronise, free.
  * (launchSPT / launchWSTL) */
 apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp);
+
+/* Largest capacity of a plan (int32 positions, whole tiles below 2^31). */
+#define APSEP_MAX_KEYS 2147479552LL
 
 /* Largest n apsep_run_noalloc accepts (2^22 keys). */
 #define APSEP_NOALLOC_MAX_KEYS 4194304

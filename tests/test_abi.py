@@ -60,6 +60,8 @@ def test_argument_validation_without_device(built_lib):
     assert lib.apsep_plan_create(ctypes.byref(h), 0, 5, 10) == _lib.APSEP_EINVAL
     assert lib.apsep_plan_create(ctypes.byref(h), 0, 0, -1) == _lib.APSEP_EINVAL
     assert lib.apsep_plan_create(ctypes.byref(h), 0, 0, 1 << 40) == _lib.APSEP_EINVAL
+    # int32 positions: the largest capacity keeps the last whole tile below 2^31
+    assert lib.apsep_plan_create(ctypes.byref(h), 0, 0, 2147479552 + 1) == _lib.APSEP_EINVAL
     assert lib.apsep_run(None, None, None, 5, None) == _lib.APSEP_EINVAL
     assert lib.apsep_plan_destroy(None) == _lib.APSEP_OK
     assert lib.apsep_plan_check(None, None) == _lib.APSEP_EINVAL
