@@ -634,6 +634,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             if (lt<INCL>(v[j], v[k])) rk = lb + j;
                         res[k] = rk;
                     }
+                    // the first key answers the previous lane's last key when that qualifies
+                    if (lane > 0 && b_adj) res[0] = lb - 1;
                 }
 #pragma unroll
                 for (int k = 0; k < IPT; k++)
@@ -727,7 +729,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     for (int k = 4; k >= 0; k--) {
 #pragma unroll
                         for (int i2 = 0; i2 < 2; i2++) {
-                            const T m = __shfl_sync(FULL, tab[k], p[i2] & 31);
+                            const T m = __shfl_sync(FULL, tab[k], p[i2]);  // p stays in [0, 31]
                             if (act[i2] && !lt<INCL>(m, q[i2])) p[i2] -= 1 << k;
                         }
                     }
@@ -738,11 +740,18 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             atomicOr(err, ERR_INTERNAL);
                             p[i2] = 0;
                         }
+                    // lane p's entries share one swizzle: word (p*IPT | j) ^ x
+                    int pb[2], px[2];
+#pragma unroll
+                    for (int i2 = 0; i2 < 2; i2++) {
+                        pb[i2] = p[i2] * IPT;
+                        px[i2] = (pb[i2] >> 3) & 0x1C;
+                    }
 #pragma unroll
                     for (int s2 = IPT / 2; s2 > 0; s2 >>= 1) {
 #pragma unroll
                         for (int i2 = 0; i2 < 2; i2++)
-                            if (act[i2] && lt<INCL>(sSM[swz(p[i2] * IPT + j[i2] + s2)], q[i2])) j[i2] += s2;
+                            if (act[i2] && lt<INCL>(sSM[(pb[i2] | (j[i2] + s2)) ^ px[i2]], q[i2])) j[i2] += s2;
                     }
 #pragma unroll
                     for (int i2 = 0; i2 < 2; i2++)
