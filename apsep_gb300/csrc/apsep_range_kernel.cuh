@@ -715,51 +715,51 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 // passes lane 0: it ends on the nearest qualifying lane p (invariant: the
                 // answer lane is <= p and after each step p - answer < 2^k).  In lane p,
                 // the suffix minima qualify on a prefix [0, j] and key j is the answer.
-                auto resolve2 = [&](int e0, bool a0, int e1, bool a1) {
-                    const int e[2] = {e0, e1};
-                    const bool act[2] = {a0, a1};
-                    T q[2];
-                    int p[2];
+                auto resolve3 = [&](int e0, bool a0, int e1, bool a1, int e2, bool a2) {
+                    const int e[3] = {e0, e1, e2};
+                    const bool act[3] = {a0, a1, a2};
+                    T q[3];
+                    int p[3];
 #pragma unroll
-                    for (int i2 = 0; i2 < 2; i2++) {
+                    for (int i2 = 0; i2 < 3; i2++) {
                         q[i2] = act[i2] ? V[swz(e[i2])] : KeyTraits<T>::pad();
                         p[i2] = act[i2] ? e[i2] / IPT - 1 : 0;
                     }
 #pragma unroll
                     for (int k = 4; k >= 0; k--) {
 #pragma unroll
-                        for (int i2 = 0; i2 < 2; i2++) {
+                        for (int i2 = 0; i2 < 3; i2++) {
                             const T m = __shfl_sync(FULL, tab[k], p[i2]);  // p stays in [0, 31]
                             if (act[i2] && !lt<INCL>(m, q[i2])) p[i2] -= 1 << k;
                         }
                     }
-                    int j[2] = {0, 0};
+                    int j[3] = {0, 0, 0};
 #pragma unroll
-                    for (int i2 = 0; i2 < 2; i2++)
+                    for (int i2 = 0; i2 < 3; i2++)
                         if (act[i2] && p[i2] < 0) {  // cannot happen (see the invariant); stay in bounds
                             atomicOr(err, ERR_INTERNAL);
                             p[i2] = 0;
                         }
                     // lane p's entries share one swizzle: word (p*IPT | j) ^ x
-                    int pb[2], px[2];
+                    int pb[3], px[3];
 #pragma unroll
-                    for (int i2 = 0; i2 < 2; i2++) {
+                    for (int i2 = 0; i2 < 3; i2++) {
                         pb[i2] = p[i2] * IPT;
                         px[i2] = (pb[i2] >> 3) & 0x1C;
                     }
 #pragma unroll
                     for (int s2 = IPT / 2; s2 > 0; s2 >>= 1) {
 #pragma unroll
-                        for (int i2 = 0; i2 < 2; i2++)
+                        for (int i2 = 0; i2 < 3; i2++)
                             if (act[i2] && lt<INCL>(sSM[(pb[i2] | (j[i2] + s2)) ^ px[i2]], q[i2])) j[i2] += s2;
                     }
 #pragma unroll
-                    for (int i2 = 0; i2 < 2; i2++)
+                    for (int i2 = 0; i2 < 3; i2++)
                         if (act[i2]) O[swz(e[i2])] = tile_base + p[i2] * IPT + j[i2];
                 };
                 const int xmax = (int)__reduce_max_sync(FULL, (unsigned)cx);
-                const int rounds = (xtot + 63) >> 6;
-                if (xmax > 2 * rounds + 1) {
+                const int rounds = (xtot + 95) / 96;
+                if (xmax > 3 * rounds + 1) {
                     // spread the queries evenly: an ordered list of X keys
                     int tot_unused;
                     int off = warp_excl_sum(cx, tot_unused);
@@ -770,20 +770,24 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         sList[off++] = (int16_t)(lane * IPT + k);
                     }
                     __syncwarp();
-                    for (int b0 = 0; b0 < xtot; b0 += 64) {
-                        const bool a0 = b0 + lane < xtot, a1 = b0 + 32 + lane < xtot;
-                        resolve2(a0 ? (int)sList[b0 + lane] : 0, a0, a1 ? (int)sList[b0 + 32 + lane] : 0, a1);
+                    for (int b0 = 0; b0 < xtot; b0 += 96) {
+                        const bool a0 = b0 + lane < xtot, a1 = b0 + 32 + lane < xtot, a2 = b0 + 64 + lane < xtot;
+                        resolve3(a0 ? (int)sList[b0 + lane] : 0, a0, a1 ? (int)sList[b0 + 32 + lane] : 0, a1,
+                                 a2 ? (int)sList[b0 + 64 + lane] : 0, a2);
                     }
                 } else {
                     unsigned m = xm;
-                    for (int rd = 0; rd < xmax; rd += 2) {
+                    for (int rd = 0; rd < xmax; rd += 3) {
                         const bool a0 = m != 0;
                         const int k0 = a0 ? __ffs(m) - 1 : 0;
                         m &= m - 1;
                         const bool a1 = m != 0;
                         const int k1 = a1 ? __ffs(m) - 1 : 0;
                         m &= m - 1;
-                        resolve2(lane * IPT + k0, a0, lane * IPT + k1, a1);
+                        const bool a2 = m != 0;
+                        const int k2 = a2 ? __ffs(m) - 1 : 0;
+                        m &= m - 1;
+                        resolve3(lane * IPT + k0, a0, lane * IPT + k1, a1, lane * IPT + k2, a2);
                     }
                 }
             }
