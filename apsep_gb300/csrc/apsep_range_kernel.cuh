@@ -189,6 +189,23 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
     return m ? row + 31 - __clz(m) : -2;
 }
 
+// The nearest range at or below `hi` whose minimum qualifies for q, or -1:
+// the ranges of hi's group, then the minima of earlier groups, 32 per step.
+// Warp-cooperative; every range and group it reads has published.
+template <typename T, bool INCL>
+__device__ __noinline__ int nearest_range(T q, int hi, const RangeArgs& a) {
+    if (hi < 0) return -1;
+    auto rmin = [&](int i) { return state_key<T>(&a.s.range_state[i]); };
+    const int g = hi >> 5;
+    const int rr = ballot_last<T, INCL>(g * 32, hi, q, rmin);
+    if (rr >= 0) return rr;
+    for (int ghi = g - 1; ghi >= 0; ghi -= 32) {
+        const int gg = ballot_last<T, INCL>(0, ghi, q, [&](int i) { return state_key<T>(&a.s.group_state[i]); });
+        if (gg >= 0) return ballot_last<T, INCL>(gg * 32, gg * 32 + 31, q, rmin);
+    }
+    return -1;
+}
+
 // ---------------------------------------------------------------------------
 // Range minima -> exclusive prefix minima.
 //
@@ -1080,18 +1097,33 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 const T m = __shfl_sync(FULL, win, i2);
                 if (want && rp < 0 && r - 1 - i2 >= 0 && lt<INCL>(m, q)) rp = r - 1 - i2;
             }
+            {  // no range of the window qualifies: the nearest one below it, key by key
+                unsigned nw = __ballot_sync(FULL, want && rp < 0);
+                while (nw) {
+                    const int f = __ffs(nw) - 1;
+                    nw &= nw - 1;
+                    const int found = nearest_range<T, INCL>(__shfl_sync(FULL, q, f), r - 33, a);
+                    if (lane == f) rp = found;
+                }
+            }
             int ans = -2;  // -2: not found yet
             if (want && rp >= 0) {
-                const uint32_t tn = __ldcg(&a.s.top_cnt[rp]);
-                const int cnt = (int)(tn & 0xffu);
-                const T* tk = (const T*)a.s.top_key + (size_t)rp * kTopEntries;
-                int lo = 0, hi = cnt;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (lt<INCL>(__ldcg(&tk[mid]), q)) lo = mid + 1;
-                    else hi = mid;
+                // rp's published stack top in one round of loads: entries increase from
+                // the bottom, so the qualifying ones form a bottom part
+                const int cnt = (int)(__ldcg(&a.s.top_cnt[rp]) & 0xffu);
+                const uint4* tk = reinterpret_cast<const uint4*>((const T*)a.s.top_key + (size_t)rp * kTopEntries);
+                uint4 tw[kTopEntries / 4];
+#pragma unroll
+                for (int k = 0; k < kTopEntries / 4; k++) tw[k] = __ldcg(&tk[k]);
+                int nq = 0;
+#pragma unroll
+                for (int k = 0; k < kTopEntries / 4; k++) {
+                    const uint32_t wb[4] = {tw[k].x, tw[k].y, tw[k].z, tw[k].w};
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        if (4 * k + c < cnt && lt<INCL>(KeyTraits<T>::from_bits(wb[c]), q)) nq = 4 * k + c + 1;
                 }
-                if (lo > 0) ans = __ldcg(&a.s.top_pos[(size_t)rp * kTopEntries + lo - 1]);
+                if (nq > 0) ans = __ldcg(&a.s.top_pos[(size_t)rp * kTopEntries + nq - 1]);
             }
             unsigned fb = __ballot_sync(FULL, want && ans == -2);
             while (fb) {
@@ -1222,8 +1254,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             a.s.ctr->range_counter = 0;
             a.s.ctr->done = 0;
             a.s.ctr->finished = 0;
-            a.s.ctr->epoch = epoch >= EPOCH_LIMIT ? 1u : epoch + 1u;
-            __threadfence();
+            a.s.ctr->epoch = epoch >= EPOCH_LIMIT ? 1u : epoch + 1u;  // (the launch's end publishes these)
         }
     }
     last = __shfl_sync(FULL, last, 0);
