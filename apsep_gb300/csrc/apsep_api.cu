@@ -144,6 +144,7 @@ apsep_status apsep_plan_create(apsep_plan** out, apsep_dtype dtype, apsep_cmp cm
     memset(&c0, 0, sizeof(c0));
     c0.epoch = 1;
     if (cudaMemset(p->scratch, 0, total) != cudaSuccess ||
+        cudaMemset(p->rs.group_min, 0xff, group_min_bytes()) != cudaSuccess ||
         cudaMemcpy(p->rs.ctr, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(p->scratch);
         delete p;

@@ -25,6 +25,9 @@ template <> struct KeyTraits<int32_t> {
     __device__ __forceinline__ static int32_t vmin(int32_t a, int32_t b) { return min(a, b); }
     __device__ __forceinline__ static uint32_t bits(int32_t a) { return (uint32_t)a; }
     __device__ __forceinline__ static int32_t from_bits(uint32_t b) { return (int32_t)b; }
+    // order-preserving map to unsigned (for unsigned atomic minima) and back
+    __device__ __forceinline__ static uint32_t ord(int32_t a) { return (uint32_t)a ^ 0x80000000u; }
+    __device__ __forceinline__ static int32_t from_ord(uint32_t o) { return (int32_t)(o ^ 0x80000000u); }
 };
 template <> struct KeyTraits<float> {
     __device__ __forceinline__ static float pad() { return __int_as_float(0x7f800000); }  // +inf
@@ -33,6 +36,14 @@ template <> struct KeyTraits<float> {
     __device__ __forceinline__ static float vmin(float a, float b) { return fminf(a, b); }
     __device__ __forceinline__ static uint32_t bits(float a) { return __float_as_uint(a); }
     __device__ __forceinline__ static float from_bits(uint32_t b) { return __uint_as_float(b); }
+    // order-preserving map to unsigned: negatives reversed below the positives
+    __device__ __forceinline__ static uint32_t ord(float a) {
+        const uint32_t b = __float_as_uint(a);
+        return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    }
+    __device__ __forceinline__ static float from_ord(uint32_t o) {
+        return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+    }
 };
 
 // lt(a, b): "a qualifies as the answer for query b".  INCL=false is the
@@ -151,6 +162,10 @@ __device__ __forceinline__ uint32_t atom_add_acq_rel_u32(uint32_t* p, uint32_t v
     uint32_t old;
     asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
     return old;
+}
+// Fire-and-forget atomic minimum (relaxed, gpu scope).
+__device__ __forceinline__ void red_min_u64(uint64_t* p, uint64_t v) {
+    asm volatile("red.relaxed.gpu.global.min.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
     uint32_t v;

@@ -28,7 +28,7 @@ struct alignas(64) Counters {
     uint32_t done;           // warps finished in the current run
     uint32_t epoch;          // tag of the current run's status words, 1..EPOCH_LIMIT
     uint32_t err;            // ERR_* bits, sticky until read
-    uint32_t finished;       // groups of 32 ranges that published their minimum in the current run
+    uint32_t finished;       // ranges that published their minimum in the current run
     uint32_t pad[11];
 };
 
@@ -36,10 +36,9 @@ struct alignas(64) Counters {
 // array of apsep_run_noalloc) by carve_scratch().
 struct RangeScratch {
     Counters* ctr;
-    uint32_t* group_cnt;    // [max_ranges/32] ranges of each group of 32 done in this run
-    uint64_t* group_state;  // [max_ranges/32] tag<<32 | key bits: min of a finished group
-    uint32_t* group_pre;    // [max_ranges/32] key bits: min of the groups before (once cta_ready says so)
-    uint32_t* cta_ready;    // [kMaxCtas * kReadyStride] epoch whose group_pre is complete, one line per CTA
+    uint64_t* group_min;    // [max_ranges/32] atomic min of (EPOCH_LIMIT - epoch) << 32 | ordered key
+                            //   over each group of 32 ranges; all-ones when created
+    uint32_t* cta_ready;    // [kMaxCtas * kReadyStride] epoch in which every range has published, one line per CTA
     uint64_t* range_state;  // [max_ranges] tag<<32 | key bits: min of a finished range
     void* top_key;          // [max_ranges * kTopEntries] key: top of each range's final stack, bottom first
     int32_t* top_pos;       // [max_ranges * kTopEntries] their positions
@@ -61,7 +60,7 @@ constexpr int kTopEntries = 32;           // stack entries each range publishes 
 
 // Byte offsets of the scratch arrays for `capacity` keys (256-byte aligned).
 struct ScratchOffsets {
-    size_t gcnt, gstate, gpre, ready, state, topk, topp, topc, tmin, cmin, flag, mask, total;
+    size_t gmin, ready, state, topk, topp, topc, tmin, cmin, flag, mask, total;
     int64_t cap_tiles;
 };
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -70,10 +69,8 @@ constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
     const int64_t cap = capacity > 0 ? capacity : 1;
     o.cap_tiles = (cap + kMinTileKeys - 1) / kMinTileKeys + 1;
     const size_t cap_chunks = (size_t)(cap + 31) / 32 + kMaxTileKeys / 32;
-    o.gcnt = align256(sizeof(Counters));  // the control region: Counters + group counters
-    o.gstate = align256(o.gcnt + (size_t)(kMaxRanges / 32) * 4);
-    o.gpre = align256(o.gstate + (size_t)(kMaxRanges / 32) * 8);
-    o.ready = align256(o.gpre + (size_t)(kMaxRanges / 32) * 4);
+    o.gmin = align256(sizeof(Counters));
+    o.ready = align256(o.gmin + (size_t)(kMaxRanges / 32) * 8);
     o.state = align256(o.ready + (size_t)kMaxCtas * kReadyStride * 4);
     o.topk = align256(o.state + (size_t)kMaxRanges * 8);
     o.topp = align256(o.topk + (size_t)kMaxRanges * kTopEntries * 4);
@@ -86,9 +83,10 @@ constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
     return o;
 }
 
-// The control region (Counters + group counters) must start zeroed; a run
-// leaves it zeroed, a run that timed out may not (apsep_plan_check clears it).
-constexpr size_t control_bytes() { return align256(sizeof(Counters)) + (size_t)(kMaxRanges / 32) * 4; }
+// The counters must start zeroed; a run leaves them zeroed, a run that timed
+// out may not (apsep_plan_check clears them, keeping the epoch).
+constexpr size_t control_bytes() { return sizeof(Counters); }
+constexpr size_t group_min_bytes() { return (size_t)(kMaxRanges / 32) * 8; }
 
 // Bytes of scratch for `capacity` keys; when base != nullptr also fills *s.
 size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s);

@@ -8,7 +8,7 @@
 // the scratch this engine needs (control block, look-back words, tile and
 // chunk minima) lives in one file-scope __device__ array below, sized for at
 // most APSEP_NOALLOC_MAX_KEYS keys.  Every GPU that loads this library holds
-// that array (2,837,760 bytes) until the process exits.
+// that array (2,836,736 bytes) until the process exits.
 //
 // Host code must not pass the array's name to a kernel: on the host it is
 // only a stand-in symbol.  The first call on each device looks up the
@@ -85,6 +85,9 @@ apsep_status scratch_for_current_device(void** out) {
         memset(&c0, 0, sizeof(c0));
         c0.epoch = 1;
         if (cudaMemcpy(p, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) return APSEP_ECUDA;
+        RangeScratch rs0;
+        carve_scratch(p, kMaxKeys, &rs0);
+        if (cudaMemset(rs0.group_min, 0xff, group_min_bytes()) != cudaSuccess) return APSEP_ECUDA;
         if (range_prepare(kConfig) != cudaSuccess) return APSEP_ECUDA;
         g_addr[dev] = p;
     }
@@ -110,11 +113,10 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
 
     RangeScratch rs;
     carve_scratch(base, kMaxKeys, &rs);
-    // The range and group counters must start at zero; a completed run leaves
-    // them so, this also covers a run that never completed.
+    // The range counters must start at zero; a completed run leaves them so,
+    // this also covers a run that never completed.
     if (cudaMemsetAsync(rs.ctr, 0, 2 * sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess ||
-        cudaMemsetAsync(&rs.ctr->finished, 0, sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess ||
-        cudaMemsetAsync(rs.group_cnt, 0, (size_t)(kMaxRanges / 32) * 4, (cudaStream_t)stream) != cudaSuccess)
+        cudaMemsetAsync(&rs.ctr->finished, 0, sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess)
         return APSEP_ECUDA;
 
     const TileConfig tc = kTileConfigs[kConfig];

@@ -16,9 +16,7 @@ size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s) {
     if (base && s) {
         char* b = (char*)base;
         s->ctr = (Counters*)b;
-        s->group_cnt = (uint32_t*)(b + o.gcnt);
-        s->group_state = (uint64_t*)(b + o.gstate);
-        s->group_pre = (uint32_t*)(b + o.gpre);
+        s->group_min = (uint64_t*)(b + o.gmin);
         s->cta_ready = (uint32_t*)(b + o.ready);
         s->range_state = (uint64_t*)(b + o.state);
         s->top_key = b + o.topk;

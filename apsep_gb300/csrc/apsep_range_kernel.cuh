@@ -75,22 +75,29 @@ constexpr size_t kernel_smem_bytes() { return WLayout<IPT>::kBytes * WPC + 1024 
 
 __device__ __forceinline__ uint32_t make_tag(uint32_t epoch, uint32_t flag) { return (epoch << 2) | flag; }
 
+// Key of a group word (the low half of an atomic minimum over ordered keys).
+template <typename T>
+__device__ __forceinline__ T group_key(const uint64_t* w) {
+    return KeyTraits<T>::from_ord((uint32_t)__ldcg((const unsigned long long*)w));
+}
+
+// Key of a range word (tag << 32 | key bits).
+template <typename T>
+__device__ __forceinline__ T state_key(const uint64_t* w) {
+    return KeyTraits<T>::from_bits((uint32_t)__ldcg((const unsigned long long*)w));
+}
+
 // ---------------------------------------------------------------------------
 // Warp-cooperative search: the rightmost position p < limit with
 // lt(d_in[p], q), or -1 (-2 if the published minima contradict each other).
 // Descends a five-level min hierarchy, 32 entries per ballot: groups of 32
-// ranges (group_state) -> ranges (range_state) -> tiles of a range
+// ranges (group_min) -> ranges (range_state) -> tiles of a range
 // (tile_min) -> 32-key chunks of a tile (chunk_min) -> keys, so an answer
 // any distance away costs a handful of dependent L2 reads.  Every range
 // before the one holding limit-1, and every group before that range's group,
 // must have published; so must the tiles and chunks below limit-1.  Reads of
 // the published arrays go to L2 (ld.cg); the keys are read-only.
 // ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ T state_key(const uint64_t* w) {
-    return KeyTraits<T>::from_bits((uint32_t)__ldcg((const unsigned long long*)w));
-}
-
 // Rightmost index i in [lo, hi] (hi - lo < 32) whose minimum qualifies, or -1.
 template <typename T, bool INCL, typename Load>
 __device__ __forceinline__ int ballot_last(int lo, int hi, T q, Load load) {
@@ -172,7 +179,7 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
             if (rr < 0) {
                 int gg = -1;
                 for (int hi = g - 1; hi >= 0 && gg < 0; hi -= 32)
-                    gg = ballot_last<T, INCL>(0, hi, q, [&](int i) { return state_key<T>(&a.s.group_state[i]); });
+                    gg = ballot_last<T, INCL>(0, hi, q, [&](int i) { return group_key<T>(&a.s.group_min[i]); });
                 if (gg < 0) return -1;
                 rr = ballot_last<T, INCL>(gg * 32, min(gg * 32 + 31, a.num_ranges - 1), q, rmin);
                 if (rr < 0) return -2;
@@ -200,7 +207,7 @@ __device__ __noinline__ int nearest_range(T q, int hi, const RangeArgs& a) {
     const int rr = ballot_last<T, INCL>(g * 32, hi, q, rmin);
     if (rr >= 0) return rr;
     for (int ghi = g - 1; ghi >= 0; ghi -= 32) {
-        const int gg = ballot_last<T, INCL>(0, ghi, q, [&](int i) { return state_key<T>(&a.s.group_state[i]); });
+        const int gg = ballot_last<T, INCL>(0, ghi, q, [&](int i) { return group_key<T>(&a.s.group_min[i]); });
         if (gg >= 0) return ballot_last<T, INCL>(gg * 32, gg * 32 + 31, q, rmin);
     }
     return -1;
@@ -209,74 +216,45 @@ __device__ __noinline__ int nearest_range(T q, int hi, const RangeArgs& a) {
 // ---------------------------------------------------------------------------
 // Range minima -> exclusive prefix minima.
 //
-// Ranges form groups of 32.  Publishing range r: one release store of its
-// minimum (range_state) and one acq_rel increment of its group's counter.
-// The last range of a group to finish publishes the group minimum
-// (group_state) and increments the count of finished groups; the last group
-// computes the exclusive prefix over groups (group_pre) and raises one ready
-// flag per CTA.  Range r then needs group_pre of its group plus the minima of
-// the earlier ranges of its group: two loads, no hot spot.
+// Publishing range r (lane 0): an atomic minimum into its group's word
+// (groups of 32 ranges), a fence, the range's tagged minimum (range_state),
+// and one relaxed increment of the count of published ranges.  The range
+// that completes the count raises one ready flag per CTA.  Range r then
+// needs the minima of the earlier ranges of its group plus those of the
+// earlier groups: one round of loads, no hot spot, and no step of the last
+// range's path waits on another range's loads.
+//
+// Group words: atomic minima of (EPOCH_LIMIT - epoch) << 32 | ordered key.
+// The current run's tag is below every older run's, so its first minimum
+// replaces an older word and the words need no reset between runs (they
+// start all-ones and are cleared again when the epoch wraps).
 //
 // Every range of a launch is resident when the launch fits the device (the
 // grid is sized from occupancy), so the ready flag always comes.  When it
 // does not come within a bound (the launch shares the device and some warps
-// have not started), range r falls back to waiting only on the groups and
-// ranges before it, all of which already run (ids are handed out in start
-// order), so no wait depends on a warp that may not start.  Every wait is
-// bounded and reports ERR_LOOKBACK_TIMEOUT when it gives up.
+// have not started), range r falls back to waiting on the tagged minima of
+// the ranges before it, all of which already run (ids are handed out in
+// start order), so no wait depends on a warp that may not start.  Every wait
+// is bounded and reports ERR_LOOKBACK_TIMEOUT when it gives up.
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ void range_publish(int r, uint32_t epoch, T rmin, const RangeArgs& a) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int g = r >> 5;
     const uint32_t tag = (epoch << 2) | FLAG_AGG;
     int last = 0;
     if (lane == 0 && r != a.skip_publish_range) {
-        // release: this range's tile words (written by all lanes, ordered by
-        // the caller's __syncwarp) before the minimum
-        st_release_u64(&a.s.range_state[r], ((uint64_t)tag << 32) | KeyTraits<T>::bits(rmin));
-        const int members = min(32, a.num_ranges - g * 32);
-        last = atom_add_acq_rel_u32(&a.s.group_cnt[g], 1u) == (uint32_t)(members - 1);
+        red_min_u64(&a.s.group_min[r >> 5], ((uint64_t)(EPOCH_LIMIT - epoch) << 32) | KeyTraits<T>::ord(rmin));
+        // release: this range's words (every lane's, ordered by the caller's
+        // __syncwarp) and the group minimum before the range minimum and the count
+        __threadfence();
+        __stcg((unsigned long long*)&a.s.range_state[r], ((uint64_t)tag << 32) | KeyTraits<T>::bits(rmin));
+        last = atomicAdd(&a.s.ctr->finished, 1u) == (uint32_t)(a.num_ranges - 1);
+        if (last) __threadfence();  // acquire: every range's publication
     }
     if (!__shfl_sync(FULL, last, 0)) return;
-    // last of its group: every member's range_state is visible (acquire above)
-    const int ri = g * 32 + lane;
-    T v = ri < a.num_ranges ? state_key<T>(&a.s.range_state[ri]) : KeyTraits<T>::pad();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = KeyTraits<T>::vmin(v, __shfl_xor_sync(FULL, v, o));
-    const int ngroups = (a.num_ranges + 31) >> 5;
-    int glast = 0;
-    if (lane == 0) {
-        a.s.group_cnt[g] = 0;  // re-armed for the next run
-        st_release_u64(&a.s.group_state[g], ((uint64_t)tag << 32) | KeyTraits<T>::bits(v));
-        glast = atom_add_acq_rel_u32(&a.s.ctr->finished, 1u) == (uint32_t)(ngroups - 1);
-    }
-    if (!__shfl_sync(FULL, glast, 0)) return;
-    // last group: exclusive prefix over the groups (at most 128, four per lane)
-    T gv[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int gi = lane * 4 + k;
-        gv[k] = gi < ngroups ? state_key<T>(&a.s.group_state[gi]) : KeyTraits<T>::pad();
-    }
-    T tot = KeyTraits<T>::vmin(KeyTraits<T>::vmin(gv[0], gv[1]), KeyTraits<T>::vmin(gv[2], gv[3]));
-    T incl = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const T u = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl = KeyTraits<T>::vmin(incl, u);
-    }
-    T run = __shfl_up_sync(FULL, incl, 1);
-    if (lane == 0) run = KeyTraits<T>::pad();  // group 0 has no prefix (never read)
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int gi = lane * 4 + k;
-        if (gi < ngroups) a.s.group_pre[gi] = KeyTraits<T>::bits(run);
-        run = KeyTraits<T>::vmin(run, gv[k]);
-    }
     __syncwarp();
-    __threadfence();
+    __threadfence();  // release to the flags' readers
     for (int c = lane; c < (int)gridDim.x; c += 32) a.s.cta_ready[(size_t)c * kReadyStride] = epoch;
 }
 
@@ -289,13 +267,33 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
     p = KeyTraits<T>::pad();
     has_p = r > 0;
     if (r == 0) return;
+    const uint32_t* flag = &a.s.cta_ready[(size_t)blockIdx.x * kReadyStride];
+    // every range has published: earlier ranges of the group, earlier groups
+    auto from_ready = [&]() {
+        const int ri = g * 32 + lane;
+        T m = ri < r ? state_key<T>(&a.s.range_state[ri]) : KeyTraits<T>::pad();
+        const uint32_t gtag = EPOCH_LIMIT - epoch;
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < kMaxRanges / 32 / 32; k++) {
+            const int gi = lane + 32 * k;
+            if (gi < g) {
+                const uint64_t w = __ldcg((const unsigned long long*)&a.s.group_min[gi]);
+                bad = bad || (uint32_t)(w >> 32) != gtag;
+                m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_ord((uint32_t)w));
+            }
+        }
+        if (bad) atomicOr(&a.s.ctr->err, ERR_INTERNAL);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
+        p = m;
+    };
     // 1. the ready flag of this CTA (one line, polled by one lane per warp)
     int ready = 0;
     if (lane == 0) {
         const uint32_t bound = min(a.spin_limit, 1u << 16);
-        const uint32_t* f = &a.s.cta_ready[(size_t)blockIdx.x * kReadyStride];
         for (uint32_t s = 0;; s++) {
-            if (ld_acquire_u32(f) == epoch) {
+            if (ld_acquire_u32(flag) == epoch) {
                 ready = 1;
                 break;
             }
@@ -305,29 +303,14 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
     }
     __syncwarp();  // lane 0's acquire before the other lanes' loads
     if (__shfl_sync(FULL, ready, 0)) {
-        const int ri = g * 32 + lane;
-        T m = ri < r ? state_key<T>(&a.s.range_state[ri]) : KeyTraits<T>::pad();
-        if (lane == 0 && g > 0) m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_bits(__ldcg(&a.s.group_pre[g])));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
-        p = m;
+        from_ready();
         return;
     }
-    // 2. fallback: wait for the earlier groups and the earlier ranges of this group
+    // 2. fallback: wait for the tagged minima of the earlier ranges (or the flag)
     for (uint32_t spins = 0;; spins++) {
         bool ok = true;
         T m = KeyTraits<T>::pad();
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int gi = lane * 4 + k;
-            if (gi < g) {
-                const uint64_t w = ld_acquire_u64(&a.s.group_state[gi]);
-                if ((uint32_t)(w >> 32) != tag) ok = false;
-                m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_bits((uint32_t)w));
-            }
-        }
-        const int ri = g * 32 + lane;
-        if (ri < r) {
+        for (int ri = lane; ri < r; ri += 32) {
             const uint64_t w = ld_acquire_u64(&a.s.range_state[ri]);
             if ((uint32_t)(w >> 32) != tag) ok = false;
             m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_bits((uint32_t)w));
@@ -336,6 +319,11 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
             p = m;
+            return;
+        }
+        if (__shfl_sync(FULL, lane == 0 ? (int)(ld_acquire_u32(flag) == epoch) : 0, 0)) {
+            __syncwarp();
+            from_ready();
             return;
         }
         if (spins >= a.spin_limit) {
@@ -358,6 +346,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     constexpr int MW = kMaxTileKeys / 32;  // flag-mask words per tile in global
     static_assert(IPT == 8 || IPT == 16, "IPT must be 8 or 16");
     static_assert((K & (K - 1)) == 0, "the stack ring needs a power-of-two size");
+    static_assert(K % 32 == 0 && K <= WT, "a whole-tile push copies the tile's last K keys, 32 per step");
     constexpr unsigned FULL = 0xffffffffu;
 
     extern __shared__ unsigned char smem_raw[];
@@ -610,12 +599,11 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         for (int j = 0; j < IPT; j++) a.d_out[tile_base + j * 32 + lane] = O[swz(j * 32 + lane)];
                     }
                     const int base_idx = stk_hi;  // entry of tile key e: base_idx + e
-                    if (lane * IPT >= WT - K) {
 #pragma unroll
-                        for (int k = 0; k < IPT; k++) {
-                            sStkV[(base_idx + lane * IPT + k) & (K - 1)] = v[k];
-                            sStkP[(base_idx + lane * IPT + k) & (K - 1)] = lb + k;
-                        }
+                    for (int h = 0; h < K / 32; h++) {  // the tile's last K keys, one per lane and step
+                        const int e = WT - K + h * 32 + lane;
+                        sStkV[(base_idx + e) & (K - 1)] = V[swz(e)];
+                        sStkP[(base_idx + e) & (K - 1)] = tile_base + e;
                     }
                     stk_hi = base_idx + WT;
                     stk_lo = stk_hi - K;
@@ -1260,7 +1248,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     last = __shfl_sync(FULL, last, 0);
     if (last && epoch >= EPOCH_LIMIT) {  // once per 2^30 runs: stale words could alias
         for (int i = lane; i < a.s.max_ranges; i += 32) a.s.range_state[i] = 0;
-        for (int i = lane; i < a.s.max_ranges / 32; i += 32) a.s.group_state[i] = 0;
+        for (int i = lane; i < a.s.max_ranges / 32; i += 32) a.s.group_min[i] = ~0ull;
         for (int i = lane; i < kMaxCtas; i += 32) a.s.cta_ready[(size_t)i * kReadyStride] = 0;
     }
 }
