@@ -31,7 +31,7 @@ namespace {
 constexpr int64_t kMaxKeys = APSEP_NOALLOC_MAX_KEYS;
 constexpr size_t kBytes = scratch_offsets(kMaxKeys).total;  // the same layout a plan uses
 
-constexpr int kConfig = 0;                 // 8 warps per CTA, 512-key warp tiles
+constexpr int kConfig = 0;                 // 16 warps per CTA, 512-key warp tiles
 constexpr uint32_t kSpinLimit = 1u << 22;  // bound on every device-side wait
 constexpr int kMaxDevices = 64;
 

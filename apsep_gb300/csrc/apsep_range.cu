@@ -7,7 +7,7 @@
 namespace apsep {
 
 const TileConfig kTileConfigs[kNumTileConfigs] = {
-    {8, 16},  // 8 warps per CTA, 512-key warp tiles
+    {16, 16},  // 16 warps per CTA (one CTA per SM), 512-key warp tiles
     {8, 8},   // 8 warps per CTA, 256-key warp tiles
 };
 

@@ -46,6 +46,7 @@ namespace apsep {
 
 constexpr int kStages = 3;      // TMA ring depth per warp (tiles)
 constexpr int kStackCap = 64;   // range-stack entries kept per warp
+constexpr int kXQueries = 3;    // cross-lane queries per lane and round (32 * 4 keys per round)
 constexpr int kDefCap = 64;     // deferred keys listed in shared memory per range
 constexpr int kCapCap = 16;     // capped keys listed in shared memory per range
 
@@ -335,7 +336,7 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
 }
 
 template <typename T, int IPT, int WPC, bool INCL, bool SEG>
-__global__ void __launch_bounds__(WPC * 32, (IPT >= 16 ? 2 : 3))
+__global__ void __launch_bounds__(WPC * 32, (IPT >= 16 ? (WPC >= 16 ? 1 : 2) : 3))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
     using L = WLayout<IPT>;
@@ -715,56 +716,57 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     const T u = __shfl_up_sync(FULL, tab[k - 1], 1 << (k - 1));
                     tab[k] = lane >= (1 << (k - 1)) ? KeyTraits<T>::vmin(tab[k - 1], u) : tab[k - 1];
                 }
-                // One query per lane and round.  A key e of lane ql = e / IPT is an X key
+                // Up to NQ queries per lane and round.  A key e of lane ql = e / IPT is an X key
                 // only when some lane before ql qualifies, so the lifting below never
                 // passes lane 0: it ends on the nearest qualifying lane p (invariant: the
                 // answer lane is <= p and after each step p - answer < 2^k).  In lane p,
                 // the suffix minima qualify on a prefix [0, j] and key j is the answer.
-                auto resolve3 = [&](int e0, bool a0, int e1, bool a1, int e2, bool a2) {
-                    const int e[3] = {e0, e1, e2};
-                    const bool act[3] = {a0, a1, a2};
-                    T q[3];
-                    int p[3];
+                constexpr int NQ = kXQueries;
+                auto resolve = [&](const int (&e)[NQ], const bool (&act)[NQ]) {
+                    T q[NQ];
+                    int p[NQ];
 #pragma unroll
-                    for (int i2 = 0; i2 < 3; i2++) {
+                    for (int i2 = 0; i2 < NQ; i2++) {
                         q[i2] = act[i2] ? V[swz(e[i2])] : KeyTraits<T>::pad();
                         p[i2] = act[i2] ? e[i2] / IPT - 1 : 0;
                     }
 #pragma unroll
                     for (int k = 4; k >= 0; k--) {
 #pragma unroll
-                        for (int i2 = 0; i2 < 3; i2++) {
+                        for (int i2 = 0; i2 < NQ; i2++) {
                             const T m = __shfl_sync(FULL, tab[k], p[i2]);  // p stays in [0, 31]
                             if (act[i2] && !lt<INCL>(m, q[i2])) p[i2] -= 1 << k;
                         }
                     }
-                    int j[3] = {0, 0, 0};
+                    int j[NQ];
 #pragma unroll
-                    for (int i2 = 0; i2 < 3; i2++)
+                    for (int i2 = 0; i2 < NQ; i2++) j[i2] = 0;
+#pragma unroll
+                    for (int i2 = 0; i2 < NQ; i2++)
                         if (act[i2] && p[i2] < 0) {  // cannot happen (see the invariant); stay in bounds
                             atomicOr(err, ERR_INTERNAL);
                             p[i2] = 0;
                         }
                     // lane p's entries share one swizzle: word (p*IPT | j) ^ x
-                    int pb[3], px[3];
+                    int pb[NQ], px[NQ];
 #pragma unroll
-                    for (int i2 = 0; i2 < 3; i2++) {
+                    for (int i2 = 0; i2 < NQ; i2++) {
                         pb[i2] = p[i2] * IPT;
                         px[i2] = (pb[i2] >> 3) & 0x1C;
                     }
 #pragma unroll
                     for (int s2 = IPT / 2; s2 > 0; s2 >>= 1) {
 #pragma unroll
-                        for (int i2 = 0; i2 < 3; i2++)
+                        for (int i2 = 0; i2 < NQ; i2++)
                             if (act[i2] && lt<INCL>(sSM[(pb[i2] | (j[i2] + s2)) ^ px[i2]], q[i2])) j[i2] += s2;
                     }
 #pragma unroll
-                    for (int i2 = 0; i2 < 3; i2++)
+                    for (int i2 = 0; i2 < NQ; i2++)
                         if (act[i2]) O[swz(e[i2])] = tile_base + p[i2] * IPT + j[i2];
                 };
                 const int xmax = (int)__reduce_max_sync(FULL, (unsigned)cx);
-                const int rounds = (xtot + 95) / 96;
-                if (xmax > 3 * rounds + 1) {
+                const int rounds = (xtot + 32 * NQ - 1) / (32 * NQ);
+                if (xmax > NQ * rounds + 1) {
                     // spread the queries evenly: an ordered list of X keys
                     int tot_unused;
                     int off = warp_excl_sum(cx, tot_unused);
@@ -775,24 +777,28 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         sList[off++] = (int16_t)(lane * IPT + k);
                     }
                     __syncwarp();
-                    for (int b0 = 0; b0 < xtot; b0 += 96) {
-                        const bool a0 = b0 + lane < xtot, a1 = b0 + 32 + lane < xtot, a2 = b0 + 64 + lane < xtot;
-                        resolve3(a0 ? (int)sList[b0 + lane] : 0, a0, a1 ? (int)sList[b0 + 32 + lane] : 0, a1,
-                                 a2 ? (int)sList[b0 + 64 + lane] : 0, a2);
+                    for (int b0 = 0; b0 < xtot; b0 += 32 * NQ) {
+                        int e[NQ];
+                        bool act[NQ];
+#pragma unroll
+                        for (int i2 = 0; i2 < NQ; i2++) {
+                            act[i2] = b0 + 32 * i2 + lane < xtot;
+                            e[i2] = act[i2] ? (int)sList[b0 + 32 * i2 + lane] : 0;
+                        }
+                        resolve(e, act);
                     }
                 } else {
                     unsigned m = xm;
-                    for (int rd = 0; rd < xmax; rd += 3) {
-                        const bool a0 = m != 0;
-                        const int k0 = a0 ? __ffs(m) - 1 : 0;
-                        m &= m - 1;
-                        const bool a1 = m != 0;
-                        const int k1 = a1 ? __ffs(m) - 1 : 0;
-                        m &= m - 1;
-                        const bool a2 = m != 0;
-                        const int k2 = a2 ? __ffs(m) - 1 : 0;
-                        m &= m - 1;
-                        resolve3(lane * IPT + k0, a0, lane * IPT + k1, a1, lane * IPT + k2, a2);
+                    for (int rd = 0; rd < xmax; rd += NQ) {
+                        int e[NQ];
+                        bool act[NQ];
+#pragma unroll
+                        for (int i2 = 0; i2 < NQ; i2++) {
+                            act[i2] = m != 0;
+                            e[i2] = lane * IPT + (act[i2] ? __ffs(m) - 1 : 0);
+                            m &= m - 1;
+                        }
+                        resolve(e, act);
                     }
                 }
             }
@@ -860,14 +866,16 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     const int e = act ? (int)sList[lane] : 0;
                     const int ans = search(act ? V[swz(e)] : KeyTraits<T>::pad(), act);
                     if (act) O[swz(e)] = ans >= 0 ? ans : -2;  // -2: a miss, flagged by the key's lane
-                    __syncwarp();
-                    unsigned m = sm;
-                    while (m) {
-                        const int k = __ffs(m) - 1;
-                        m &= m - 1;
-                        if (O[swz(lane * IPT + k)] == -2) {
-                            O[swz(lane * IPT + k)] = -1;
-                            cm |= 1u << k;
+                    if (__any_sync(FULL, act && ans < 0)) {      // (only once the stack has dropped entries)
+                        __syncwarp();
+                        unsigned m = sm;
+                        while (m) {
+                            const int k = __ffs(m) - 1;
+                            m &= m - 1;
+                            if (O[swz(lane * IPT + k)] == -2) {
+                                O[swz(lane * IPT + k)] = -1;
+                                cm |= 1u << k;
+                            }
                         }
                     }
                 } else {
@@ -1296,7 +1304,7 @@ inline cudaError_t prepare_mode(int cfg, int* per_sm) {
             if (rr[q] != cudaSuccess) return rr[q];                                    \
     }
     switch (cfg) {
-    case 0: P_(16, 8); break;
+    case 0: P_(16, 16); break;
     case 1: P_(8, 8); break;
     default: return cudaErrorInvalidValue;
     }
@@ -1315,7 +1323,7 @@ inline cudaError_t launch_mode(int dtype, int incl, int cfg, RangeArgs& a, const
         return incl ? launch_t<float, IPT, WPC, true, SEG>(a, mi, mo, st, max_warps)        \
                     : launch_t<float, IPT, WPC, false, SEG>(a, mi, mo, st, max_warps);
     switch (cfg) {
-    case 0: L_(16, 8);
+    case 0: L_(16, 16);
     case 1: L_(8, 8);
     }
 #undef L_
