@@ -24,10 +24,13 @@ a time, copy in, apsep_run, copy out, synchronise.
 
 Device-resident requests (`ResidentServer`): when the keys are produced on
 the GPU (or uploaded by the client ahead of time), the pool is a ring of
-keys and answers in HBM that requests occupy in arrival order.  A batch is a
-contiguous span of arrived requests and runs in place, one segmented launch
-with no copies; `resident_loop` is its per-request baseline (one apsep_run
-per request on the same memory, synchronised).
+keys and answers in HBM that requests occupy in arrival order, each in a
+slot of whole 4-key units (16-byte aligned starts, so every launch streams
+through TMA; a batch starting mid-line would take the kernel's plain-load
+path at about half the speed).  A batch is a contiguous span of arrived
+requests and runs in place, one segmented launch with no copies;
+`resident_loop` is its per-request baseline (one apsep_run per request on the
+same memory, synchronised).
 """
 from __future__ import annotations
 
@@ -293,12 +296,21 @@ class ResidentRequest:
     t_done: float | None = None
 
 
+RESIDENT_SLOT_KEYS = 4  # ring slots are whole 4-key (16-byte) units
+
+
 class ResidentServer:
     """Requests whose keys already sit in a device ring (in arrival order).
 
     keys/answers: the ring (device tensors of equal length); requests must
-    not wrap.  Each batch is the longest run of arrived, waiting requests
-    that fits `max_batch_keys` and `max_segments`, launched in place."""
+    not wrap.  Each request occupies a slot of whole RESIDENT_SLOT_KEYS units
+    (it starts on a 16-byte boundary of the ring, so every batch does and its
+    launch streams through TMA); the up to 3 keys between a request's end and
+    the next slot must hold padding that never qualifies as an answer
+    (INT_MAX / +inf).  Each batch is the longest run of arrived, waiting
+    requests that fits `max_batch_keys` and `max_segments`, launched in place:
+    a request's segment also spans the padding after it, whose answers land in
+    the matching gap of `answers`."""
 
     def __init__(self, keys: torch.Tensor, answers: torch.Tensor, inclusive: bool = False,
                  max_batch_keys: int = 64 << 20, max_segments: int = 4096, streams: int = 2,
@@ -328,10 +340,9 @@ class ResidentServer:
 
     def _launch(self, ln, batch):
         base = batch[0].start
-        offs = [0]
-        for r in batch:
-            offs.append(offs[-1] + r.n)
-        total = offs[-1]
+        offs = [r.start - base for r in batch]
+        total = batch[-1].start + batch[-1].n - base
+        offs.append(total)
         ns = len(batch)
         ln["batch"] = batch
         with torch.cuda.stream(ln["stream"]):
@@ -343,9 +354,12 @@ class ResidentServer:
 
     def serve(self, requests: list, realtime: bool = True) -> ServeStats:
         order = sorted(requests, key=lambda r: r.start)
+        for r in order:
+            if r.start % RESIDENT_SLOT_KEYS:
+                raise ValueError("resident requests must start on a %d-key boundary of the ring" % RESIDENT_SLOT_KEYS)
         for a, b in zip(order, order[1:]):
-            if b.start != a.start + a.n:
-                raise ValueError("resident requests must lie back to back in the ring, in arrival order")
+            if not 0 <= b.start - (a.start + a.n) < RESIDENT_SLOT_KEYS:
+                raise ValueError("resident requests must fill consecutive slots of the ring, in arrival order")
         nxt = done = batches = 0
         waiting = collections.deque()
         torch.cuda.synchronize(self.device)

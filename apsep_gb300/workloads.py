@@ -83,25 +83,32 @@ def serve_requests(count: int, rate: float, seed: int = 11, lo: int = 1 << 10, h
 def resident_requests(count: int, rate: float, seed: int = 11, lo: int = 1 << 10, hi: int = 1 << 24,
                       dtype=torch.int32, device="cuda"):
     """The served workload's lengths and arrivals, keys generated in place in a
-    device ring (back to back, arrival order).  Returns (keys, answers, requests)."""
-    from .serve import ResidentRequest
+    device ring in arrival order, each request in a slot of whole 4-key units
+    (so every request starts on a 16-byte boundary; the up to 3 keys after a
+    request hold padding: INT_MAX / +inf).  Returns (keys, answers, requests)."""
+    from .serve import RESIDENT_SLOT_KEYS, ResidentRequest
 
     rng = np.random.default_rng(seed)
     lengths = segment_lengths(count, lo, hi, seed + 1)
     gaps = rng.exponential(1.0 / rate, count) if rate > 0 else np.zeros(count)
     arrivals = np.cumsum(gaps)
-    n = int(lengths.sum())
+    slots = (lengths + RESIDENT_SLOT_KEYS - 1) // RESIDENT_SLOT_KEYS * RESIDENT_SLOT_KEYS
+    starts = np.zeros(count, dtype=np.int64)
+    starts[1:] = np.cumsum(slots)[:-1]
+    n = int(slots.sum())
     g = torch.Generator(device=device)
     g.manual_seed(seed)
     if dtype == torch.int32:
         keys = torch.randint(0, 1 << 31, (n,), generator=g, device=device, dtype=torch.int64).to(torch.int32)
+        pad = float(2**31 - 1)
     else:
         u = torch.randint(0, 1 << 24, (n,), generator=g, device=device, dtype=torch.int64)
         keys = (-1e6 + u.to(torch.float64) * (2e6 / (1 << 24))).to(torch.float32)
+        pad = float("inf")
+    fill = np.concatenate([np.arange(s + L, s + S) for s, L, S in zip(starts, lengths, slots)]).astype(np.int64)
+    if fill.size:
+        keys[torch.from_numpy(fill).to(device)] = pad
     answers = torch.empty(n, dtype=torch.int32, device=device)
-    reqs, pos = [], 0
-    for i in range(count):
-        L = int(lengths[i])
-        reqs.append(ResidentRequest(rid=i, start=pos, n=L, arrival=float(arrivals[i])))
-        pos += L
+    reqs = [ResidentRequest(rid=i, start=int(starts[i]), n=int(lengths[i]), arrival=float(arrivals[i]))
+            for i in range(count)]
     return keys, answers, reqs

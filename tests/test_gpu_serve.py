@@ -85,4 +85,7 @@ def test_resident_server_matches_oracle_and_loop(dtype):
         assert np.array_equal(got[r.start:r.start + r.n], oracle.apse(k[r.start:r.start + r.n])), r.rid
     answers.fill_(-7)
     resident_loop(keys, answers, reqs, realtime=False)
-    assert np.array_equal(answers.cpu().numpy(), got)
+    loop = answers.cpu().numpy()
+    for r in reqs:
+        assert r.start % 4 == 0
+        assert np.array_equal(loop[r.start:r.start + r.n], got[r.start:r.start + r.n]), r.rid
