@@ -214,7 +214,7 @@ def test_cuda_graph_capture(plans):
 def test_lookback_timeout_is_reported_not_hung():
     """A predecessor range that never publishes: the successors' bounded
     waits give up, the run finishes, the host reads APSEP_ETIMEOUT, and the
-    next run on the same plan is correct again.  (6 tiles -> 6 one-tile ranges.)"""
+    next run on the same plan is correct again.  (48 tiles -> 48 one-tile ranges.)"""
     n = 4096 * 6
     a = dist("uniform", n, np.random.default_rng(8))
     with Plan(n, torch.int32) as plan:
