@@ -259,20 +259,25 @@ __device__ void range_publish(int r, uint32_t epoch, T rmin, const RangeArgs& a)
     for (int c = lane; c < (int)gridDim.x; c += 32) a.s.cta_ready[(size_t)c * kReadyStride] = epoch;
 }
 
+// p: the minimum over ranges [0, r); win (lane i): the minimum of range r-1-i
+// (pad below range 0), the window phase 2 searches first.
 template <typename T>
-__device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bool& has_p) {
+__device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bool& has_p, T& win) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int g = r >> 5;
     const uint32_t tag = (epoch << 2) | FLAG_AGG;
     p = KeyTraits<T>::pad();
+    win = KeyTraits<T>::pad();
     has_p = r > 0;
     if (r == 0) return;
     const uint32_t* flag = &a.s.cta_ready[(size_t)blockIdx.x * kReadyStride];
-    // every range has published: earlier ranges of the group, earlier groups
+    // every range has published: the window (it holds the group's earlier
+    // ranges) and the earlier groups, in one round of loads
     auto from_ready = [&]() {
-        const int ri = g * 32 + lane;
-        T m = ri < r ? state_key<T>(&a.s.range_state[ri]) : KeyTraits<T>::pad();
+        const int wi = r - 1 - lane;
+        win = wi >= 0 ? state_key<T>(&a.s.range_state[wi]) : KeyTraits<T>::pad();
+        T m = wi >= g * 32 ? win : KeyTraits<T>::pad();
         const uint32_t gtag = EPOCH_LIMIT - epoch;
         bool bad = false;
 #pragma unroll
@@ -320,6 +325,8 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
             p = m;
+            const int wi = r - 1 - lane;
+            win = wi >= 0 ? state_key<T>(&a.s.range_state[wi]) : KeyTraits<T>::pad();
             return;
         }
         if (__shfl_sync(FULL, lane == 0 ? (int)(ld_acquire_u32(flag) == epoch) : 0, 0)) {
@@ -1052,9 +1059,9 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         }
         __syncwarp();  // every lane's words before lane 0's release in range_publish
         range_publish<T>(r, epoch, rmin, a);
-        T P;
+        T P, win;
         bool has_p;
-        range_prefix<T>(r, epoch, a, P, has_p);
+        range_prefix<T>(r, epoch, a, P, has_p, win);
         if (lane == 0) {
             bulk_wait0();       // this range's tile stores have landed ...
             fence_proxy_async();  // ... before phase 2 overwrites flagged keys
@@ -1073,8 +1080,6 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         //    published stack (lane-parallel searches), else found by find_left.
         bool a_done = !has_p;
         const int nlist = min(def_total, kDefCap);
-        T win = KeyTraits<T>::pad();
-        bool win_loaded = false;
         for (int b0 = 0; b0 < nlist && !a_done; b0 += 32) {
             const int j = b0 + lane;
             const bool in = j < nlist;
@@ -1083,10 +1088,6 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             const bool want = in && lt<INCL>(P, q);  // (segmented: all of the range's first segment)
             if (__ballot_sync(FULL, want) != __ballot_sync(FULL, in)) a_done = true;
             if (!__any_sync(FULL, want)) break;
-            if (!win_loaded) {  // lane i: the minimum of range r - 1 - i
-                win = r - 1 - lane >= 0 ? state_key<T>(&a.s.range_state[r - 1 - lane]) : KeyTraits<T>::pad();
-                win_loaded = true;
-            }
             int rp = -1;
 #pragma unroll 4
             for (int i2 = 0; i2 < 32; i2++) {
@@ -1104,22 +1105,26 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             int ans = -2;  // -2: not found yet
             if (want && rp >= 0) {
-                // rp's published stack top in one round of loads: entries increase from
-                // the bottom, so the qualifying ones form a bottom part
+                // rp's published stack top, keys and positions in one round of loads:
+                // entries increase from the bottom, so the qualifying ones form a
+                // bottom part and the topmost of them answers
                 const int cnt = (int)(__ldcg(&a.s.top_cnt[rp]) & 0xffu);
                 const uint4* tk = reinterpret_cast<const uint4*>((const T*)a.s.top_key + (size_t)rp * kTopEntries);
-                uint4 tw[kTopEntries / 4];
+                const uint4* tp = reinterpret_cast<const uint4*>(a.s.top_pos + (size_t)rp * kTopEntries);
+                uint4 tw[kTopEntries / 4], pw[kTopEntries / 4];
 #pragma unroll
-                for (int k = 0; k < kTopEntries / 4; k++) tw[k] = __ldcg(&tk[k]);
-                int nq = 0;
+                for (int k = 0; k < kTopEntries / 4; k++) {
+                    tw[k] = __ldcg(&tk[k]);
+                    pw[k] = __ldcg(&tp[k]);
+                }
 #pragma unroll
                 for (int k = 0; k < kTopEntries / 4; k++) {
                     const uint32_t wb[4] = {tw[k].x, tw[k].y, tw[k].z, tw[k].w};
+                    const int pb[4] = {(int)pw[k].x, (int)pw[k].y, (int)pw[k].z, (int)pw[k].w};
 #pragma unroll
                     for (int c = 0; c < 4; c++)
-                        if (4 * k + c < cnt && lt<INCL>(KeyTraits<T>::from_bits(wb[c]), q)) nq = 4 * k + c + 1;
+                        if (4 * k + c < cnt && lt<INCL>(KeyTraits<T>::from_bits(wb[c]), q)) ans = pb[c];
                 }
-                if (nq > 0) ans = __ldcg(&a.s.top_pos[(size_t)rp * kTopEntries + nq - 1]);
             }
             unsigned fb = __ballot_sync(FULL, want && ans == -2);
             while (fb) {
