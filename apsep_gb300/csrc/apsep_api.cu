@@ -200,6 +200,7 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
     if (offsets && (nseg < 1 || (uintptr_t)offsets % 8 != 0)) return APSEP_EINVAL;
     if (n == 0) return APSEP_OK;
     if (n > p->capacity || !d_in || !d_out) return APSEP_EINVAL;
+    if ((uintptr_t)d_in % 4 != 0 || (uintptr_t)d_out % 4 != 0) return APSEP_EINVAL;  // 4-byte keys and answers
     if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_EINVAL;
     if (offsets && (ranges_overlap(offsets, (size_t)(nseg + 1) * 8, d_out, (size_t)n * 4) ||
                     ranges_overlap(offsets, (size_t)(nseg + 1) * 8, d_in, (size_t)n * 4)))
@@ -210,35 +211,43 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
     const TileConfig tc = kTileConfigs[p->cfg];
     const int B = 32 * tc.ipt;  // keys per warp tile
     const int tile_rows = B / 32;
-    const int64_t num_tiles = (n + B - 1) / B;
-    int rows = (int)(n / 32);
+    // the view: `head` virtual keys in front put it on a 16-byte boundary
+    const int vh = view_head(d_in, d_out);
+    const int head = vh > 0 ? vh : 0;
+    const int64_t nv = n + head;
+    const void* v_in = (const char*)d_in - 4 * head;
+    int32_t* v_out = d_out - head;
+    const int64_t num_tiles = (nv + B - 1) / B;
+    int rows = (int)(nv / 32);
     CUtensorMap mi, mo;
     memset(&mi, 0, sizeof(mi));
     memset(&mo, 0, sizeof(mo));
-    const bool aligned = ((uintptr_t)d_in % 16 == 0) && ((uintptr_t)d_out % 16 == 0);
-    if (!aligned || rows < tile_rows) rows = 0;
+    if (vh < 0 || rows < tile_rows) rows = 0;
     if (rows > 0) {
-        if (!encode_rows(&mi, d_in, rows, tile_rows, p->dtype) || !encode_rows(&mo, d_out, rows, tile_rows, 0))
+        if (!encode_rows(&mi, v_in, rows, tile_rows, p->dtype) || !encode_rows(&mo, v_out, rows, tile_rows, 0))
             return APSEP_ECUDA;
     }
     RangeArgs a;
-    a.d_in = d_in;
-    a.d_out = d_out;
-    a.n = (int)n;
+    a.d_in = v_in;
+    a.d_out = v_out;
+    a.n = (int)nv;
+    a.head = head;
     a.num_tiles = (int)num_tiles;
     a.tiles_per_range = 0;
     a.num_ranges = 0;
     a.tma_rows = rows;
     a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
     a.skip_publish_range = p->dbg_skip_range;
+    // a single array behind a view head runs in the segmented kernel as one
+    // implicit segment (the plain single-array kernel has no view head)
     a.offsets = offsets;
-    a.nseg = offsets ? nseg : 0;
+    a.nseg = offsets ? nseg : 1;
     a.s = p->rs;
     p->dbg_skip_range = -1;  // one-shot
     p->dbg_spin_limit = 0;
     const int incl = cmp == APSEP_LE ? 1 : 0;
-    cudaError_t e = offsets ? launch_range_segmented(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
-                            : launch_range(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream);
+    cudaError_t e = offsets || head ? launch_range_segmented(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
+                                    : launch_range(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }
 

@@ -99,12 +99,25 @@ struct RangeArgs {
     int tiles_per_range;
     int num_ranges;
     int tma_rows;            // floor(n/32): rows covered by the tensor maps (0 = no TMA)
+    int head;                // 0..3 virtual keys in front of the array (d_in, d_out and n
+                             //   include them) so that the TMA view starts 16-byte aligned;
+                             //   never read or written, answers are relative to them
     uint32_t spin_limit;     // bound on every device-side wait (polls)
     int skip_publish_range;  // fault injection: this range never publishes (-1 = off)
     const int64_t* offsets;  // segmented runs: nseg + 1 segment offsets into d_in; else nullptr
     int nseg;
     RangeScratch s;
 };
+
+// The TMA view of a run: the number of virtual keys (0..3) in front of d_in
+// that put the view on a 16-byte boundary, or -1 when the input and the output
+// sit at different offsets within 16 bytes (no common view: plain loads and
+// stores throughout).  Tile 0, which holds the virtual keys, always takes the
+// plain path, so nothing in front of the arrays is touched.
+inline int view_head(const void* d_in, const void* d_out) {
+    const int hi = (int)((uintptr_t)d_in % 16 / 4), ho = (int)((uintptr_t)d_out % 16 / 4);
+    return hi == ho ? hi : -1;
+}
 
 // A kernel configuration: warps per CTA x keys per lane (a warp's tile is 32*ipt keys).
 struct TileConfig {

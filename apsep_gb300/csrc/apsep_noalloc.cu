@@ -104,6 +104,7 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
     if (n > kMaxKeys) return APSEP_EINVAL;  // beyond the static scratch: use a plan
     if (n == 0) return APSEP_OK;
     if (!d_in || !d_out) return APSEP_EINVAL;
+    if ((uintptr_t)d_in % 4 != 0 || (uintptr_t)d_out % 4 != 0) return APSEP_EINVAL;
     const uintptr_t a0 = (uintptr_t)d_in, b0 = (uintptr_t)d_out, bytes = (uintptr_t)n * 4;
     if (a0 < b0 + bytes && b0 < a0 + bytes) return APSEP_EINVAL;
 
@@ -122,25 +123,36 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
     const TileConfig tc = kTileConfigs[kConfig];
     const int B = 32 * tc.ipt;  // keys per warp tile
     const int tile_rows = B / 32;
-    int rows = (int)(n / 32);
+    // the view: `head` virtual keys in front put it on a 16-byte boundary
+    const int vh = view_head(d_in, d_out);
+    const int head = vh > 0 ? vh : 0;
+    const int64_t nv = n + head;
+    const void* v_in = (const char*)d_in - 4 * head;
+    int32_t* v_out = d_out - head;
+    int rows = (int)(nv / 32);
     CUtensorMap mi, mo;
     memset(&mi, 0, sizeof(mi));
     memset(&mo, 0, sizeof(mo));
-    if (a0 % 16 != 0 || b0 % 16 != 0 || rows < tile_rows) rows = 0;
-    if (rows > 0 && (!encode(&mi, d_in, rows, tile_rows, dtype) || !encode(&mo, d_out, rows, tile_rows, 0)))
+    if (vh < 0 || rows < tile_rows) rows = 0;
+    if (rows > 0 && (!encode(&mi, v_in, rows, tile_rows, dtype) || !encode(&mo, v_out, rows, tile_rows, 0)))
         return APSEP_ECUDA;
 
     RangeArgs a;
-    a.d_in = d_in;
-    a.d_out = d_out;
-    a.n = (int)n;
-    a.num_tiles = (int)((n + B - 1) / B);
+    a.d_in = v_in;
+    a.d_out = v_out;
+    a.n = (int)nv;
+    a.head = head;
+    a.num_tiles = (int)((nv + B - 1) / B);
     a.tiles_per_range = 0;
     a.num_ranges = 0;
     a.tma_rows = rows;
     a.spin_limit = kSpinLimit;
     a.skip_publish_range = -1;
     a.s = rs;
-    cudaError_t e = launch_range(dtype, cmp == APSEP_LE ? 1 : 0, kConfig, a, mi, mo, (cudaStream_t)stream);
+    a.offsets = nullptr;  // (behind a view head: the segmented kernel, one implicit segment)
+    a.nseg = 1;
+    const int incl = cmp == APSEP_LE ? 1 : 0;
+    cudaError_t e = head ? launch_range_segmented(dtype, incl, kConfig, a, mi, mo, (cudaStream_t)stream)
+                         : launch_range(dtype, incl, kConfig, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }

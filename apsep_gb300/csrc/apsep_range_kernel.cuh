@@ -158,7 +158,7 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
     {  // 1. the row holding limit-1, positions below limit
         const int row = t * B + c * 32;
         const int p = row + lane;
-        const bool ok = p < limit && lt<INCL>(__ldg(&d_in[p]), q);
+        const bool ok = p < limit && p >= a.head && lt<INCL>(__ldg(&d_in[p]), q);
         const unsigned m = __ballot_sync(0xffffffffu, ok);
         if (m) return row + 31 - __clz(m);
     }
@@ -193,7 +193,7 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
         if (cc < 0) return -2;
     }
     const int row = s * B + cc * 32;
-    const unsigned m = __ballot_sync(0xffffffffu, lt<INCL>(__ldg(&d_in[row + lane]), q));
+    const unsigned m = __ballot_sync(0xffffffffu, row + lane >= a.head && lt<INCL>(__ldg(&d_in[row + lane]), q));
     return m ? row + 31 - __clz(m) : -2;
 }
 
@@ -380,6 +380,14 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     T* tile_min_w = (T*)a.s.tile_min;
     T* chunk_min_w = (T*)a.s.chunk_min;
     uint32_t* err = &a.s.ctr->err;
+    // The view's virtual keys: only the segmented kernel has them (a single
+    // array off a 16-byte boundary runs there as one implicit segment).
+    const int head = SEG ? a.head : 0;
+    // Segment offsets (positions in the array); with no offsets array, one segment.
+    auto seg_off = [&](int i) -> int64_t {
+        return a.offsets ? (int64_t)__ldg(&a.offsets[i]) : (i == 0 ? (int64_t)0 : (int64_t)(a.n - head));
+    };
+    auto seg_idx = [&](int pos) { return a.offsets ? seg_find(a.offsets, a.nseg, pos, err) : 0; };
 
     // One claim per CTA: its warps take WPC consecutive range ids, in the order
     // the CTAs start (so every range a warp may wait on belongs to a started CTA).
@@ -403,7 +411,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         const int t0 = r * a.tiles_per_range;
         const int t1 = min(t0 + a.tiles_per_range, a.num_tiles);
         const int ntr = t1 - t0;
-        auto tile_full = [&](int t) { return a.tma_rows > 0 && (t + 1) * W <= a.tma_rows; };
+        auto tile_full = [&](int t) { return a.tma_rows > 0 && (t + 1) * W <= a.tma_rows && (t > 0 || head == 0); };
         if (lane == 0) {
             for (int i = 0; i < kStages && i < ntr; i++)
                 if (tile_full(t0 + i)) {
@@ -424,11 +432,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         int seg_cur = 0, cur_start = 0, next_b = INT_MAX;
         int first_start = 0, first_end = INT_MAX;  // the segment holding the range's first key
         if constexpr (SEG) {
-            if (r == 0 && lane == 0 && (a.offsets[0] != 0 || a.offsets[a.nseg] != (int64_t)a.n))
+            if (r == 0 && lane == 0 && a.offsets && (a.offsets[0] != 0 || a.offsets[a.nseg] != (int64_t)(a.n - head)))
                 atomicOr(err, ERR_BAD_OFFSETS);
-            seg_cur = seg_find(a.offsets, a.nseg, t0 * WT, err);
-            cur_start = (int)min(max(__ldg(&a.offsets[seg_cur]), (int64_t)0), (int64_t)INT_MAX);
-            next_b = (int)min(max(__ldg(&a.offsets[seg_cur + 1]), (int64_t)0), (int64_t)INT_MAX);
+            // offsets are positions in the array; the view adds `head` virtual keys in
+            // front (they fall in segment 0, and no answer of theirs is written)
+            seg_cur = seg_idx(max(t0 * WT - head, 0));
+            cur_start = (int)min(max(seg_off(seg_cur), (int64_t)0) + head, (int64_t)INT_MAX);
+            next_b = (int)min(max(seg_off(seg_cur + 1), (int64_t)0) + head, (int64_t)INT_MAX);
             first_start = cur_start;
             first_end = next_b;
         }
@@ -450,8 +460,12 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 for (int j = 0; j < IPT; j++) {
                     const int e = j * 32 + lane;
                     const int g = tile_base + e;
-                    V[swz(e)] = g < a.n ? d_in[g] : KeyTraits<T>::pad();
+                    V[swz(e)] = g < a.n && (!head || g >= head) ? d_in[g] : KeyTraits<T>::pad();
                 }
+                // A view head makes tile 0 plain while tile kStages streams into its
+                // slot: the plain tile completes the slot barrier's phase by itself.
+                // (Any other plain tile is the array's last: its slot is not reused.)
+                if (head && lane == 0 && a.tma_rows > 0) mbar_arrive(&bar[slot]);
             }
             if (lane == 0) bulk_wait_read0();  // the previous tile's store has read O
             __syncwarp();
@@ -468,7 +482,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     __syncwarp();
                     for (int it = 0; it <= a.nseg / 32 + 1; it++) {  // ends once past off[nseg]
                         const int idx = seg_cur + 1 + lane;
-                        const int64_t b = idx <= a.nseg ? __ldg(&a.offsets[idx]) : (int64_t)INT_MAX;
+                        const int64_t b = idx <= a.nseg ? seg_off(idx) + head : (int64_t)INT_MAX;
                         const bool in = b >= tile_base && b < tile_end;
                         if (in) atomicOr(&bm[(int)(b - tile_base) >> 5], 1u << ((int)(b - tile_base) & 31));
                         const int cnt = __popc(__ballot_sync(FULL, b < tile_end));
@@ -558,7 +572,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         }
                     } else {
 #pragma unroll
-                        for (int j = 0; j < IPT; j++) a.d_out[tile_base + j * 32 + lane] = -1;
+                        for (int j = 0; j < IPT; j++)
+                            if (!head || tile_base + j * 32 + lane >= head) a.d_out[tile_base + j * 32 + lane] = -1;
                     }
                     if (lane == 31) {
                         sStkV[stk_lo & (K - 1)] = v[IPT - 1];
@@ -604,7 +619,9 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         }
                     } else {
 #pragma unroll
-                        for (int j = 0; j < IPT; j++) a.d_out[tile_base + j * 32 + lane] = O[swz(j * 32 + lane)];
+                        for (int j = 0; j < IPT; j++)
+                            if (!head || tile_base + j * 32 + lane >= head)
+                                a.d_out[tile_base + j * 32 + lane] = O[swz(j * 32 + lane)];
                     }
                     const int base_idx = stk_hi;  // entry of tile key e: base_idx + e
 #pragma unroll
@@ -973,7 +990,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 #pragma unroll
                 for (int j = 0; j < IPT; j++) {
                     const int e = j * 32 + lane;
-                    if (e < valid_keys) a.d_out[tile_base + e] = O[swz(e)];
+                    if (e < valid_keys && (!head || tile_base + e >= head)) a.d_out[tile_base + e] = O[swz(e)];
                 }
             }
 
@@ -1138,7 +1155,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             if (want) {
                 if (ans < 0) atomicOr(err, ERR_INTERNAL);
-                else a.d_out[pos] = SEG ? seg_rel(ans, first_start) : ans;
+                else if (!head || pos >= head) a.d_out[pos] = SEG ? seg_rel(ans, first_start) : ans;
             }
         }
         if (!a_done && def_total > kDefCap) {
@@ -1155,7 +1172,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 for (int w = 0; w < W && !a_done; w++) {
                     const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
                     const int pos = t * WT + w * 32 + lane;
-                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from);
+                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from && (!head || pos >= head));
                     if (!pend) continue;
                     const T q = ((pend >> lane) & 1u) ? __ldg(&d_in[pos]) : KeyTraits<T>::pad();
                     if (mixed) {  // deferred and capped keys: a full search each
@@ -1166,7 +1183,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             const int found = find_left<T, WT, INCL>(__shfl_sync(FULL, q, f), pf, d_in, tile_min_r,
                                                                      chunk_min_r, a);
                             int sf = 0;
-                            if constexpr (SEG) sf = (int)__ldg(&a.offsets[seg_find(a.offsets, a.nseg, pf, err)]);
+                            if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
                             if (lane == f) {
                                 if (found < -1) atomicOr(err, ERR_INTERNAL);
                                 else a.d_out[pos] = SEG ? seg_rel(found, sf) : found;
@@ -1212,7 +1229,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             const int found = find_left<T, WT, INCL>(__ldg(&d_in[pos]), pos, d_in, tile_min_r, chunk_min_r, a);
             if (lane == 0) {
                 if (found < 0) atomicOr(err, ERR_INTERNAL);
-                else a.d_out[pos] = SEG ? seg_rel(found, sCapS[j]) : found;
+                else if (!head || pos >= head) a.d_out[pos] = SEG ? seg_rel(found, sCapS[j]) : found;
             }
         }
         if (cap_total > kCapCap) {
@@ -1224,7 +1241,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 for (int w = 0; w < W; w++) {
                     const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
                     const int pos = t * WT + w * 32 + lane;
-                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from);
+                    unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from && (!head || pos >= head));
                     while (pend) {
                         const int f = __ffs(pend) - 1;
                         pend &= pend - 1;
@@ -1232,7 +1249,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         const int found =
                             find_left<T, WT, INCL>(__ldg(&d_in[pf]), pf, d_in, tile_min_r, chunk_min_r, a);
                         int sf = 0;
-                        if constexpr (SEG) sf = (int)__ldg(&a.offsets[seg_find(a.offsets, a.nseg, pf, err)]);
+                        if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
                         if (lane == f) {
                             if (found < -1) atomicOr(err, ERR_INTERNAL);
                             else a.d_out[pf] = SEG ? seg_rel(found, sf) : found;

@@ -19,7 +19,7 @@ cudaError_t launch_range_segmented(int dtype, int incl, int cfg, RangeArgs& a, c
     int max_warps = 0;
     const cudaError_t e = range_max_warps(cfg, &max_warps);
     if (e != cudaSuccess) return e;
-    if (!a.offsets || a.nseg < 1) return cudaErrorInvalidValue;
+    if (a.nseg < 1 || (!a.offsets && a.nseg != 1)) return cudaErrorInvalidValue;  // no offsets: one segment
     return launch_mode<true>(dtype, incl, cfg, a, mi, mo, st, max_warps);
 }
 

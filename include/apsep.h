@@ -83,9 +83,12 @@ apsep_status apsep_plan_destroy(apsep_plan* plan);
 
 /* Enqueue one run on `stream`: d_out[0..n) <- APSE(d_in[0..n)).  Asynchronous,
  * no allocation, no synchronisation, so it can be captured in a CUDA graph.
- * n == 0 is a no-op.  d_in/d_out need no particular alignment (16-byte
- * aligned arrays take the TMA path).  Runs on one plan must not overlap in
- * time (serialise them on one stream).  (runSPT / runWSTL) */
+ * n == 0 is a no-op.  d_in/d_out must be 4-byte aligned (else
+ * APSEP_EINVAL).  Arrays at the same offset within 16 bytes stream through
+ * TMA (off a 16-byte boundary: behind 1-3 virtual keys, in the segmented
+ * kernel as one segment); arrays at different offsets take plain loads and
+ * stores.  Runs on one plan must not overlap in time (serialise them on one
+ * stream).  (runSPT / runWSTL) */
 apsep_status apsep_run(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, void* stream);
 
 /* apsep_run with the comparator chosen per call (runSPT<...,INCL>). */

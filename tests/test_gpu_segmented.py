@@ -117,6 +117,28 @@ def test_segments_spanning_many_ranges(dist):
         check(plan, a, offs)
 
 
+@pytest.mark.parametrize("shift", [1, 2, 3])
+def test_misaligned_batch_base(shift):
+    """A batch whose keys and answers start 4*shift bytes past a 16-byte
+    boundary (the view adds virtual keys in front; offsets stay relative to
+    the batch).  The words before the answers stay untouched."""
+    rng = np.random.default_rng(shift)
+    lengths = np.array([int(x) for x in np.exp(rng.uniform(np.log(1), np.log(300000), 60))], dtype=np.int64)
+    lengths[:5] = [0, 1, 2, 3, 5]
+    a, offs = batch(lengths, ["uniform", "desc", "asc", "runs", "dup16"], rng)
+    n = a.shape[0]
+    xb = torch.zeros(n + 4, dtype=torch.int32, device="cuda")
+    xb[shift:shift + n] = torch.from_numpy(a).cuda()
+    for le in (False, True):
+        ob = torch.full((n + 4,), POISON, dtype=torch.int32, device="cuda")
+        with Plan(n, torch.int32, inclusive=le) as plan:
+            plan.run_segmented(xb[shift:shift + n], torch.from_numpy(offs).cuda(), out=ob[shift:shift + n])
+            plan.check()
+        got = ob.cpu().numpy()
+        assert np.array_equal(got[shift:shift + n], oracle.apse_segmented(a, offs, le))
+        assert (got[:shift] == POISON).all() and (got[shift + n:] == POISON).all()
+
+
 def test_one_segment_equals_single_run():
     rng = np.random.default_rng(15)
     a = keys("uniform", 1000003, rng)

@@ -162,6 +162,52 @@ def test_unaligned_buffers(plans, offset):
             assert np.array_equal(run_gpu(plan, a, offset=offset), oracle.apse(a)), (name, n)
 
 
+@pytest.mark.parametrize("oin,oout", [(1, 1), (2, 2), (3, 3), (1, 2), (3, 0), (0, 2)])
+@pytest.mark.parametrize("le", [False, True])
+def test_misaligned_views(plans, oin, oout, le):
+    """Buffers off their 16-byte alignment.  Equal offsets stream through TMA
+    behind 1-3 virtual keys (tile 0 takes plain loads and stores); unequal
+    offsets take the plain path throughout.  Nothing outside out[0:n] is
+    written (the words around it stay poisoned)."""
+    rng = np.random.default_rng(oin * 7 + oout + (100 if le else 0))
+    plan = plans[torch.int32]
+    for n in (1, 511, 5000, 3_000_001):  # 3e6 keys: multi-tile ranges, whole-tile early paths
+        for name in ("uniform", "desc", "asc", "dup16"):
+            a = dist(name, n, rng)
+            xb = torch.zeros(n + 4, dtype=torch.int32, device="cuda")
+            xb[oin:oin + n] = torch.from_numpy(a).cuda()
+            ob = torch.full((n + 4,), int(POISON), dtype=torch.int32, device="cuda")
+            plan.run(xb[oin:oin + n], out=ob[oout:oout + n], n=n, inclusive=le)
+            plan.check()
+            got = ob.cpu().numpy()
+            assert np.array_equal(got[oout:oout + n], oracle.apse(a, le)), (name, n)
+            assert (got[:oout] == POISON).all() and (got[oout + n:] == POISON).all(), (name, n)
+
+
+def test_misaligned_float_view(plans):
+    rng = np.random.default_rng(41)
+    plan = plans[torch.float32]
+    n = 1_000_003
+    a = (rng.integers(0, 1 << 24, n) * (2e6 / (1 << 24)) - 1e6).astype(np.float32)
+    xb = torch.zeros(n + 4, dtype=torch.float32, device="cuda")
+    xb[2:2 + n] = torch.from_numpy(a).cuda()
+    ob = torch.full((n + 4,), int(POISON), dtype=torch.int32, device="cuda")
+    plan.run(xb[2:2 + n], out=ob[2:2 + n])
+    plan.check()
+    got = ob.cpu().numpy()
+    assert np.array_equal(got[2:2 + n], oracle.apse(a))
+    assert (got[:2] == POISON).all() and (got[2 + n:] == POISON).all()
+
+
+def test_pointer_not_4_byte_aligned_is_einval(plans):
+    plan = plans[torch.int32]
+    x = torch.zeros(1000, dtype=torch.int32, device="cuda")
+    o = torch.zeros(1000, dtype=torch.int32, device="cuda")
+    lib = _lib.load()
+    assert lib.apsep_run(plan._h, x.data_ptr() + 2, o.data_ptr(), 100, None) == _lib.APSEP_EINVAL
+    assert lib.apsep_run(plan._h, x.data_ptr(), o.data_ptr() + 1, 100, None) == _lib.APSEP_EINVAL
+
+
 @pytest.mark.parametrize("name", ["uniform", "desc", "asc", "dup16"])
 def test_full_size_2_25(plans, name):
     n = 1 << 25

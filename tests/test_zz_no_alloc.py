@@ -14,6 +14,8 @@ import numpy as np
 import pytest
 import torch
 
+import oracle
+
 from apsep_gb300 import Plan, _lib
 
 pytestmark = pytest.mark.gpu
@@ -46,6 +48,21 @@ def test_noalloc_matches_plan_on_two_calls_in_a_row():
             assert _noalloc(x, out, n, dtype, cmp) == _lib.APSEP_OK
             torch.cuda.synchronize()
             assert torch.equal(out.cpu(), want)
+
+
+def test_noalloc_misaligned_view_at_full_capacity():
+    """The largest no-alloc size behind a 3-key view head (the view then holds
+    max + 3 keys, which the static scratch must still cover)."""
+    n = _lib.NOALLOC_MAX_KEYS
+    a = np.random.default_rng(77).integers(0, 1 << 31, n, dtype=np.int64).astype(np.int32)
+    xb = torch.zeros(n + 4, dtype=torch.int32, device="cuda")
+    xb[3:3 + n] = torch.from_numpy(a).cuda()
+    ob = torch.full((n + 4,), -7, dtype=torch.int32, device="cuda")
+    assert _noalloc(xb[3:3 + n], ob[3:3 + n], n, _lib.INT32, _lib.LT) == _lib.APSEP_OK
+    torch.cuda.synchronize()
+    got = ob.cpu().numpy()
+    assert np.array_equal(got[3:3 + n], oracle.apse(a))
+    assert (got[:3] == -7).all() and got[3 + n] == -7
 
 
 def test_noalloc_refuses_sizes_beyond_its_static_scratch():
