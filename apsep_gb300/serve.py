@@ -26,8 +26,7 @@ Device-resident requests (`ResidentServer`): when the keys are produced on
 the GPU (or uploaded by the client ahead of time), the pool is a ring of
 keys and answers in HBM that requests occupy in arrival order, each in a
 slot of whole 4-key units (16-byte aligned starts, so every launch streams
-through TMA; a batch starting mid-line would take the kernel's plain-load
-path at about half the speed).  A batch is a contiguous span of arrived
+through TMA from its first tile).  A batch is a contiguous span of arrived
 requests and runs in place, one segmented launch with no copies;
 `resident_loop` is its per-request baseline (one apsep_run per request on the
 same memory, synchronised).
@@ -305,7 +304,8 @@ class ResidentServer:
     keys/answers: the ring (device tensors of equal length); requests must
     not wrap.  Each request occupies a slot of whole RESIDENT_SLOT_KEYS units
     (it starts on a 16-byte boundary of the ring, so every batch does and its
-    launch streams through TMA); the up to 3 keys between a request's end and
+    launch streams through TMA from its first tile); the up to 3 keys between a
+    request's end and
     the next slot must hold padding that never qualifies as an answer
     (INT_MAX / +inf).  Each batch is the longest run of arrived, waiting
     requests that fits `max_batch_keys` and `max_segments`, launched in place:
