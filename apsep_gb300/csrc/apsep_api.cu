@@ -238,16 +238,17 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
     a.tma_rows = rows;
     a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
     a.skip_publish_range = p->dbg_skip_range;
-    // a single array behind a view head runs in the segmented kernel as one
-    // implicit segment (the plain single-array kernel has no view head)
+    // (a single array behind a view head runs in the view kernel: one implicit
+    //  segment; the plain single-array kernel has no view head)
     a.offsets = offsets;
     a.nseg = offsets ? nseg : 1;
     a.s = p->rs;
     p->dbg_skip_range = -1;  // one-shot
     p->dbg_spin_limit = 0;
     const int incl = cmp == APSEP_LE ? 1 : 0;
-    cudaError_t e = offsets || head ? launch_range_segmented(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
-                                    : launch_range(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream);
+    cudaError_t e = offsets ? launch_range_segmented(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
+                    : head  ? launch_range_view(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
+                            : launch_range(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }
 

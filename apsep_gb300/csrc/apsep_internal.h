@@ -136,6 +136,11 @@ cudaError_t range_prepare(int cfg);  // smem attributes + occupancy, current dev
 // each key's segment start.
 cudaError_t launch_range_segmented(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& map_in,
                                    const CUtensorMap& map_out, cudaStream_t stream);
+// A single array behind a view head (RangeArgs::head > 0): the segmented
+// kernel with one implicit segment and the whole-tile early paths.
+cudaError_t prepare_view(int cfg, int* ctas_per_sm);
+cudaError_t launch_range_view(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& map_in,
+                              const CUtensorMap& map_out, cudaStream_t st);
 cudaError_t prepare_segmented(int cfg, int* ctas_per_sm);
 cudaError_t range_max_warps(int cfg, int* warps);  // persistent warps of one launch, current device
 

@@ -149,10 +149,8 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
     a.spin_limit = kSpinLimit;
     a.skip_publish_range = -1;
     a.s = rs;
-    a.offsets = nullptr;  // (behind a view head: the segmented kernel, one implicit segment)
-    a.nseg = 1;
     const int incl = cmp == APSEP_LE ? 1 : 0;
-    cudaError_t e = head ? launch_range_segmented(dtype, incl, kConfig, a, mi, mo, (cudaStream_t)stream)
+    cudaError_t e = head ? launch_range_view(dtype, incl, kConfig, a, mi, mo, (cudaStream_t)stream)
                          : launch_range(dtype, incl, kConfig, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }

@@ -42,10 +42,12 @@ cudaError_t range_prepare(int cfg) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDev || cfg < 0 || cfg >= kNumTileConfigs) return cudaErrorInvalidValue;
-    int per_sm = 0;  // the smallest over both modes, so a segmented run fits too
-    e = prepare_mode<false>(cfg, &per_sm);
+    int per_sm = 0;  // the smallest over the three modes, so every run fits
+    e = prepare_mode<false, true>(cfg, &per_sm);
     if (e != cudaSuccess) return e;
     e = prepare_segmented(cfg, &per_sm);
+    if (e != cudaSuccess) return e;
+    e = prepare_view(cfg, &per_sm);
     if (e != cudaSuccess) return e;
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -77,7 +79,7 @@ cudaError_t launch_range(int dtype, int incl, int cfg, RangeArgs& a, const CUten
     if (e != cudaSuccess) return e;
     a.offsets = nullptr;
     a.nseg = 0;
-    return launch_mode<false>(dtype, incl, cfg, a, mi, mo, st, max_warps);
+    return launch_mode<false, true>(dtype, incl, cfg, a, mi, mo, st, max_warps);
 }
 
 }  // namespace apsep

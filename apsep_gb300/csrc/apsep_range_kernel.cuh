@@ -342,7 +342,7 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
     }
 }
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
 __global__ void __launch_bounds__(WPC * 32, (IPT >= 16 ? (WPC >= 16 ? 1 : 2) : 3))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
@@ -380,8 +380,9 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     T* tile_min_w = (T*)a.s.tile_min;
     T* chunk_min_w = (T*)a.s.chunk_min;
     uint32_t* err = &a.s.ctr->err;
-    // The view's virtual keys: only the segmented kernel has them (a single
-    // array off a 16-byte boundary runs there as one implicit segment).
+    // The view's virtual keys: only the segmented instantiations have them (a
+    // batch off a 16-byte boundary; a single array off one runs as one implicit
+    // segment with the whole-tile early paths, EP).
     const int head = SEG ? a.head : 0;
     // Segment offsets (positions in the array); with no offsets array, one segment.
     auto seg_off = [&](int i) -> int64_t {
@@ -543,8 +544,9 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             // included) and whose first key has no qualifying key earlier in the
             // range has no answer for any key inside the range: every key is deferred,
             // every stack entry (>= the range minimum >= the first key) is popped and
-            // the tile's last key is its only strict suffix minimum.  (Single arrays.)
-            if constexpr (!SEG) {
+            // the tile's last key is its only strict suffix minimum.  (Single arrays,
+            // also a single array behind a view head in the segmented kernel.)
+            if constexpr (EP) {
                 const T first = __shfl_sync(FULL, v[0], 0);
                 if (mono == FULL && valid_keys == WT && __all_sync(FULL, none && (lane == 0 || !b_adj)) &&
                     (!has_rmin || !lt<INCL>(rmin, first))) {
@@ -595,16 +597,19 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             // A strictly increasing tile whose first key is above the stack's top entry
             // (the range's last key): every key answers its predecessor, every key is a
             // strict suffix minimum, and the ring keeps the tile's last K keys.
-            if constexpr (!SEG && !INCL) {  // (strict comparator: adj means strictly increasing)
+            if constexpr (EP && !INCL) {  // (strict comparator: adj means strictly increasing)
                 const T first = __shfl_sync(FULL, v[0], 0);
                 if (mono == FULL && valid_keys == WT && __all_sync(FULL, adj && b_adj) && stk_hi > stk_lo &&
                     sStkV[(stk_hi - 1) & (K - 1)] < first) {
-                    const int top_pos = sStkP[(stk_hi - 1) & (K - 1)];
+                    // answers relative to the array (a view head's pads are never the
+                    // stack top here: a pad does not lie below the tile's first key)
+                    const int top_pos = sStkP[(stk_hi - 1) & (K - 1)] - head;
+                    const int hb = lb - head;
 #pragma unroll
                     for (int q4 = 0; q4 < IPT / 4; q4++)
                         *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) =
-                            make_int4(lane == 0 && q4 == 0 ? top_pos : lb + 4 * q4 - 1, lb + 4 * q4, lb + 4 * q4 + 1,
-                                      lb + 4 * q4 + 2);
+                            make_int4(lane == 0 && q4 == 0 ? top_pos : hb + 4 * q4 - 1, hb + 4 * q4, hb + 4 * q4 + 1,
+                                      hb + 4 * q4 + 2);
                     if ((lane & (TPC - 1)) == 0) __stcg(&chunk_min_w[(size_t)t * W + lane / TPC], v[0]);
                     if (lane == 0) {
                         __stcg(&a.s.tile_flag[t], 0u);
@@ -1286,7 +1291,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 // ---------------------------------------------------------------------------
 // Launch plumbing shared by the single-array and segmented translation units.
 // ---------------------------------------------------------------------------
-template <typename T, int IPT, int WPC, bool INCL, bool SEG>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
 inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo, cudaStream_t st,
                             int max_warps) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC>();
@@ -1295,14 +1300,14 @@ inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorM
     a.tiles_per_range = tpr;
     a.num_ranges = (a.num_tiles + tpr - 1) / tpr;
     const int ctas = (a.num_ranges + WPC - 1) / WPC;
-    apse_warp_kernel<T, IPT, WPC, INCL, SEG><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
+    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
     return cudaGetLastError();
 }
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
 inline cudaError_t prepare_t(int* ctas_per_sm) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC>();
-    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG>;
+    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int n = 0;
@@ -1314,14 +1319,14 @@ inline cudaError_t prepare_t(int* ctas_per_sm) {
 
 // Shared-memory attributes and occupancy of every kernel of one mode and
 // configuration (the smallest CTAs-per-SM over the four key/comparison types).
-template <bool SEG>
+template <bool SEG, bool EP>
 inline cudaError_t prepare_mode(int cfg, int* per_sm) {
 #define P_(IPT, WPC)                                                                   \
     {                                                                                  \
-        cudaError_t rr[4] = {prepare_t<int32_t, IPT, WPC, false, SEG>(per_sm),         \
-                             prepare_t<int32_t, IPT, WPC, true, SEG>(per_sm),          \
-                             prepare_t<float, IPT, WPC, false, SEG>(per_sm),           \
-                             prepare_t<float, IPT, WPC, true, SEG>(per_sm)};           \
+        cudaError_t rr[4] = {prepare_t<int32_t, IPT, WPC, false, SEG, EP>(per_sm),     \
+                             prepare_t<int32_t, IPT, WPC, true, SEG, EP>(per_sm),      \
+                             prepare_t<float, IPT, WPC, false, SEG, EP>(per_sm),       \
+                             prepare_t<float, IPT, WPC, true, SEG, EP>(per_sm)};       \
         for (int q = 0; q < 4; q++)                                                    \
             if (rr[q] != cudaSuccess) return rr[q];                                    \
     }
@@ -1334,16 +1339,16 @@ inline cudaError_t prepare_mode(int cfg, int* per_sm) {
     return cudaSuccess;
 }
 
-template <bool SEG>
+template <bool SEG, bool EP>
 inline cudaError_t launch_mode(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& mi,
                                const CUtensorMap& mo, cudaStream_t st, int max_warps) {
 #define L_(IPT, WPC)                                                                        \
     if (dtype == 0)                                                                         \
-        return incl ? launch_t<int32_t, IPT, WPC, true, SEG>(a, mi, mo, st, max_warps)      \
-                    : launch_t<int32_t, IPT, WPC, false, SEG>(a, mi, mo, st, max_warps);    \
+        return incl ? launch_t<int32_t, IPT, WPC, true, SEG, EP>(a, mi, mo, st, max_warps)  \
+                    : launch_t<int32_t, IPT, WPC, false, SEG, EP>(a, mi, mo, st, max_warps); \
     else                                                                                    \
-        return incl ? launch_t<float, IPT, WPC, true, SEG>(a, mi, mo, st, max_warps)        \
-                    : launch_t<float, IPT, WPC, false, SEG>(a, mi, mo, st, max_warps);
+        return incl ? launch_t<float, IPT, WPC, true, SEG, EP>(a, mi, mo, st, max_warps)    \
+                    : launch_t<float, IPT, WPC, false, SEG, EP>(a, mi, mo, st, max_warps);
     switch (cfg) {
     case 0: L_(16, 16);
     case 1: L_(8, 8);

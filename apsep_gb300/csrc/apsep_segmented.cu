@@ -12,15 +12,15 @@
 
 namespace apsep {
 
-cudaError_t prepare_segmented(int cfg, int* ctas_per_sm) { return prepare_mode<true>(cfg, ctas_per_sm); }
+cudaError_t prepare_segmented(int cfg, int* ctas_per_sm) { return prepare_mode<true, false>(cfg, ctas_per_sm); }
 
 cudaError_t launch_range_segmented(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& mi,
                                    const CUtensorMap& mo, cudaStream_t st) {
     int max_warps = 0;
     const cudaError_t e = range_max_warps(cfg, &max_warps);
     if (e != cudaSuccess) return e;
-    if (a.nseg < 1 || (!a.offsets && a.nseg != 1)) return cudaErrorInvalidValue;  // no offsets: one segment
-    return launch_mode<true>(dtype, incl, cfg, a, mi, mo, st, max_warps);
+    if (!a.offsets || a.nseg < 1) return cudaErrorInvalidValue;
+    return launch_mode<true, false>(dtype, incl, cfg, a, mi, mo, st, max_warps);
 }
 
 }  // namespace apsep

@@ -15,6 +15,9 @@ beside it.
              step, outside the events: a 512 MiB buffer is written and then
              read, so no line of the inputs stays cached and no dirty line of
              the flush is left for the timed kernel to write back.
+  per_distribution  median (with p10 / p90) device time per distribution,
+             and the median of the same steps back to back without the
+             flush.
   e2e        the same metric through the public API with host buffers: each
              step copies the keys from pinned host memory, runs, and copies
              the answers back, all inside the timed region.  value: the steps
@@ -190,6 +193,7 @@ def cpu_baseline(inputs: dict[str, np.ndarray], reps: int = 2) -> dict:
             times.append(time.perf_counter() - t0)
     tot = sum(times)
     return {"value": round(useful_gbs(N, tot, len(times)), 3), "unit": UNIT, "cores": 1, "kind": "port",
+            "nproc": os.cpu_count(),
             "sample": "%d passes: %d reps x {%s} at N=2^25 int32, one thread, %.1f s" %
                       (len(times), reps, ",".join(DISTS), tot)}
 
@@ -475,6 +479,17 @@ def run_ours(args) -> None:
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
 
+    # the same steps back to back without the flush (answers of the previous
+    # step may still be dirty in L2; a 2^25 input is larger than L2 anyway)
+    ev_u = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        ev_u[i][0].record(stream)
+        plan.run(d_in[DISTS[i % 4]], out=out)
+        ev_u[i][1].record(stream)
+    torch.cuda.synchronize()
+    plan.check()
+    step_ms_unflushed = [a.elapsed_time(b) for a, b in ev_u]
+
     # e2e through the public API: pinned host -> device, run, device -> host.
     # (a) serial: one step at a time on one stream (L2 flushed before each);
     # (b) pipelined: the steps in flight on three streams with two device
@@ -508,10 +523,14 @@ def run_ours(args) -> None:
     value = whole_job_gbs(N, total_ms, args.steps, world)
     per = {}
     for j, name in enumerate(DISTS):
-        ms = [step_ms[i] for i in range(args.steps) if i % 4 == j]
+        ms = sorted(step_ms[i] for i in range(args.steps) if i % 4 == j)
+        mu = sorted(step_ms_unflushed[i] for i in range(args.steps) if i % 4 == j)
         if ms:
+            pct = lambda v, q: v[min(len(v) - 1, int(q * (len(v) - 1) + 0.5))]
             per[name] = {"gbs": round(useful_gbs(N, statistics.median(ms) / 1e3), 1),
-                         "us_median": round(statistics.median(ms) * 1e3, 2)}
+                         "us_median": round(statistics.median(ms) * 1e3, 2),
+                         "us_p10": round(pct(ms, 0.1) * 1e3, 2), "us_p90": round(pct(ms, 0.9) * 1e3, 2),
+                         "us_median_unflushed": round(statistics.median(mu) * 1e3, 2)}
     peaks = measured_peaks()
     mean_s = total_ms / 1e3 / args.steps
     achieved = 8.0 * N / mean_s / 1e9
