@@ -31,6 +31,12 @@ SIGNATURES = {
     "apsep_debug_inject": ([_vp, _i32, _u32], ctypes.c_int),
     "apsep_run_noalloc": ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
     "apsep_run_segmented": ([_vp, _vp, _vp, _i64, _vp, _i32, _vp], ctypes.c_int),
+    "apsep_consumer_workspace_bytes": ([_i64], _i64),
+    "apsep_run_prev_greater": ([_vp, _vp, _vp, _i64, ctypes.c_int, _vp, _vp], ctypes.c_int),
+    "apsep_run_next_smaller": ([_vp, _vp, _vp, _i64, ctypes.c_int, _vp, _vp], ctypes.c_int),
+    "apsep_stock_span": ([_vp, _vp, _vp, _i64, _vp, _vp], ctypes.c_int),
+    "apsep_largest_rectangle": ([_vp, _vp, _i64, _vp, _vp, _vp], ctypes.c_int),
+    "apsep_cartesian_parents": ([_vp, _vp, _vp, _i64, _vp, _vp], ctypes.c_int),
 }
 
 NOALLOC_MAX_KEYS = 4194304  # APSEP_NOALLOC_MAX_KEYS in include/apsep.h

@@ -147,6 +147,45 @@ apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dty
 apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp,
                                void* stream);
 
+/* ---- Consumers of APSE ------------------------------------------------------
+ * The classic callers the reference names for its output (README.md:3,
+ * src/bench_spt_le.cu:1-3), each a few memory-bound passes around one or two
+ * runs on `plan` (whose key type they use; n <= its capacity), asynchronous
+ * on `stream` like apsep_run.  d_work: a 16-byte aligned device workspace of
+ * apsep_consumer_workspace_bytes(n) bytes, not overlapping the inputs or
+ * outputs.  Device-side errors of the inner runs surface through
+ * apsep_plan_check. */
+int64_t apsep_consumer_workspace_bytes(int64_t n);
+
+/* d_out[i] = the largest j < i with a[j] > a[i] (APSEP_LT) or a[j] >= a[i]
+ * (APSEP_LE), else -1: APSE of the order-reversed keys. */
+apsep_status apsep_run_prev_greater(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                                    void* d_work, void* stream);
+
+/* d_out[i] = the smallest j > i with a[j] < a[i] (APSEP_LT) or a[j] <= a[i]
+ * (APSEP_LE), else -1: APSE of the reversed array, mirrored back. */
+apsep_status apsep_run_next_smaller(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                                    void* d_work, void* stream);
+
+/* Stock span: d_out[i] = i - (the largest j < i with a[j] > a[i], else -1),
+ * the number of consecutive keys ending at i that are <= a[i]. */
+apsep_status apsep_stock_span(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, void* d_work,
+                              void* stream);
+
+/* Largest rectangle in a histogram of int32 heights >= 0 (an int32 plan):
+ * *d_area (device int64) = max over i of h[i] * (R - L - 1), L the previous
+ * and R the next strictly smaller index (-1 / n when none); 0 for n == 0. */
+apsep_status apsep_largest_rectangle(apsep_plan* plan, const int32_t* d_heights, int64_t n, int64_t* d_area,
+                                     void* d_work, void* stream);
+
+/* Min-rooted Cartesian tree: d_out[i] = the parent of i (-1 at the root),
+ * ties as the stack construction makes them (a later equal key becomes the
+ * right child of an earlier one).  The parent is, of the previous
+ * smaller-or-equal and the next strictly smaller key, the larger one (the
+ * next on a tie). */
+apsep_status apsep_cartesian_parents(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, void* d_work,
+                                     void* stream);
+
 /* Fault injection for failure-detection tests: in the next run, range `range`
  * (the contiguous block of tiles one persistent CTA sweeps) never publishes
  * its look-back status, and every device wait gives up after `spin_limit`

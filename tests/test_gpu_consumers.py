@@ -1,0 +1,124 @@
+"""GPU parity of the consumers (apsep_run_prev_greater, apsep_run_next_smaller,
+apsep_stock_span, apsep_largest_rectangle, apsep_cartesian_parents) through
+the C ABI, bit-exact against the CPU oracles: the monotone-stack
+restatements on small inputs, their (CPU-pinned) compositions on large ones."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import consumers as oc
+from apsep_gb300 import ApsepError, Plan, _lib, consumers
+
+pytestmark = pytest.mark.gpu
+
+
+def keys(name, n, rng, dtype=np.int32):
+    if name == "uniform":
+        a = rng.integers(-(1 << 31), 1 << 31, n, dtype=np.int64)
+    elif name == "dup16":
+        a = rng.integers(0, 16, n)
+    elif name == "desc":
+        a = np.arange(n, 0, -1)
+    elif name == "asc":
+        a = np.arange(n)
+    else:
+        raise KeyError(name)
+    if dtype == np.float32:
+        return (a % (1 << 20) * 0.25 - (1 << 17)).astype(np.float32)
+    return a.astype(np.int32)
+
+
+SIZES = [1, 2, 1000, 65543, 3_000_001]
+
+
+@pytest.fixture(scope="module")
+def plans():
+    p = {np.int32: Plan(3_000_001, torch.int32), np.float32: Plan(3_000_001, torch.float32)}
+    yield p
+    for v in p.values():
+        v.close()
+
+
+def check(got, want, what):
+    if not np.array_equal(got, want):
+        bad = int(np.flatnonzero(got != want)[0])
+        pytest.fail("%s: first mismatch at %d: got %d want %d" % (what, bad, got[bad], want[bad]))
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.float32])
+@pytest.mark.parametrize("name", ["uniform", "dup16", "desc", "asc"])
+def test_prev_greater_next_smaller_span_cartesian(plans, dtype, name):
+    rng = np.random.default_rng(sum(map(ord, name)) + (7 if dtype == np.float32 else 0))
+    plan = plans[dtype]
+    for n in SIZES:
+        a = keys(name, n, rng, dtype)
+        x = torch.from_numpy(a).cuda()
+        small = n <= 1000
+        for le in (False, True):
+            want = oc.prev_greater_stack(list(a), le) if small else oc.prev_greater(a, le)
+            check(consumers.prev_greater(x, le, plan=plan).cpu().numpy(), want, "prev_greater %s %d" % (le, n))
+            want = oc.next_smaller_stack(list(a), le) if small else oc.next_smaller(a, le)
+            check(consumers.next_smaller(x, le, plan=plan).cpu().numpy(), want, "next_smaller %s %d" % (le, n))
+        want = oc.stock_span_stack(list(a)) if small else oc.stock_span(a)
+        check(consumers.stock_span(x, plan=plan).cpu().numpy(), want, "stock_span %d" % n)
+        want = oc.cartesian_parents_stack(list(a)) if small else oc.cartesian_parents(a)
+        check(consumers.cartesian_parents(x, plan=plan).cpu().numpy(), want, "cartesian %d" % n)
+        plan.check()
+
+
+@pytest.mark.parametrize("k", [2, 1000, 1 << 30])
+def test_largest_rectangle(plans, k):
+    rng = np.random.default_rng(k)
+    for n in SIZES:
+        h = rng.integers(0, k, n).astype(np.int32)
+        want = oc.largest_rectangle_stack(list(h)) if n <= 1000 else oc.largest_rectangle(h)
+        assert consumers.largest_rectangle(torch.from_numpy(h).cuda(), plan=plans[np.int32]) == want, n
+    assert consumers.largest_rectangle(torch.tensor([2, 1, 5, 6, 2, 3], dtype=torch.int32, device="cuda")) == 10
+    plans[np.int32].check()
+
+
+def test_one_workspace_no_allocation_in_the_loop(plans):
+    rng = np.random.default_rng(9)
+    plan = plans[np.int32]
+    n = 200_003
+    work = torch.empty(consumers.workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        a = rng.integers(0, 100, n).astype(np.int32)
+        x = torch.from_numpy(a).cuda()
+        check(consumers.stock_span(x, plan=plan, work=work).cpu().numpy(), oc.stock_span(a), "span")
+        check(consumers.cartesian_parents(x, plan=plan, work=work).cpu().numpy(), oc.cartesian_parents(a), "cart")
+    plan.check()
+
+
+def test_invalid_arguments(plans):
+    lib = _lib.load()
+    plan = plans[np.int32]
+    x = torch.zeros(1000, dtype=torch.int32, device="cuda")
+    o = torch.zeros(1000, dtype=torch.int32, device="cuda")
+    w = torch.empty(consumers.workspace_bytes(1000) + 64, dtype=torch.uint8, device="cuda")
+    vp = ctypes.c_void_p
+    # workspace off a 16-byte boundary
+    assert lib.apsep_run_prev_greater(plan._h, vp(x.data_ptr()), vp(o.data_ptr()), 1000, _lib.LT,
+                                      vp(w.data_ptr() + 4), None) == _lib.APSEP_EINVAL
+    # workspace overlapping the output
+    assert lib.apsep_stock_span(plan._h, vp(x.data_ptr()), vp(o.data_ptr()), 1000, vp(o.data_ptr()),
+                                None) == _lib.APSEP_EINVAL
+    # beyond the plan's capacity
+    with Plan(10, torch.int32) as small:
+        assert lib.apsep_run_next_smaller(small._h, vp(x.data_ptr()), vp(o.data_ptr()), 1000, _lib.LT,
+                                          vp(w.data_ptr()), None) == _lib.APSEP_EINVAL
+    # the histogram needs an int32 plan
+    area = torch.zeros(1, dtype=torch.int64, device="cuda")
+    xf = torch.zeros(1000, dtype=torch.float32, device="cuda")
+    assert lib.apsep_largest_rectangle(plans[np.float32]._h, vp(xf.data_ptr()), 1000, vp(area.data_ptr()),
+                                       vp(w.data_ptr()), None) == _lib.APSEP_ENOTSUP
+    # n == 0 is a no-op (the area is 0)
+    area.fill_(7)
+    assert lib.apsep_largest_rectangle(plan._h, vp(x.data_ptr()), 0, vp(area.data_ptr()), vp(w.data_ptr()),
+                                       None) == _lib.APSEP_OK
+    torch.cuda.synchronize()
+    assert int(area.item()) == 0
+    with pytest.raises(ValueError):
+        consumers.prev_greater(x.cpu())
