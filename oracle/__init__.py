@@ -1,7 +1,8 @@
 """CPU oracle for APSE -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
-this package, and only as the checker / the timed CPU baseline.  The product
+this package, and only to verify the engine's answers / as the timed CPU
+baseline.  The product
 (apsep_gb300, libapsep.so) never imports, links or calls it.
 
 Contents

@@ -2,9 +2,9 @@
  * apsep_oracle.c -- CPU ORACLE for the All Previous Smaller Element problem.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the apsep_gb300 package,
- * libapsep.so, the C ABI) links, loads or calls this file.  It is used by the
- * tests as the checker, by __graft_entry__.smoke() as the checker, and by
- * bench.py as the timed CPU baseline ("cpu_baseline", "--impl reference").
+ * libapsep.so, the C ABI) links, loads or calls this file.  The tests and
+ * __graft_entry__.smoke() compare the engine's answers with it, and bench.py
+ * times it as the CPU baseline ("cpu_baseline", "--impl reference").
  *
  * It restates, in plain C, the reference's sequential monotone-stack oracles:
  *   - cpuApsep  (src/main.cu:102-113): strict "<", int only;
