@@ -46,6 +46,9 @@ Extra objects on the same line (one GPU only; --no-extras skips them):
              then p50/p99 latency at a Poisson offered load of half the
              server's saturated rate.  served.resident: the same stream with
              the keys already in a device ring (batches run in place).
+  consumers  previous greater, next smaller, stock span, Cartesian parents and
+             largest rectangle at N = 2^25 (apsep_gb300.consumers): time,
+             useful GB/s and the fraction of peak of all their HBM passes.
   sweep      single-array useful GB/s and roofline fraction for N = 2^14 ..
              2^30 (every second power of two), uniform and descending keys.
 
@@ -273,6 +276,53 @@ def run_batched(dev) -> dict:
             "batched_gbs": round(useful / batched_ms / 1e6, 1), "loop_gbs": round(useful / loop_ms / 1e6, 2),
             "speedup_vs_loop": round(loop_ms / batched_ms, 2), "launches": {"batched": 1, "loop": S},
             "note": "device time (CUDA events); the loop is enqueued from Python, one apsep_run per array"}
+
+
+def run_consumers(dev, peak_gbs: float) -> dict:
+    """The consumers of APSE at N = 2^25 int32 (uniform keys; heights uniform
+    in [0, 2^20) for the histogram), device time with L2 flushed.  useful GB/s
+    counts the caller's bytes (keys in, answers out); pass_bytes counts every
+    pass over HBM, workspace included, for the roofline."""
+    import torch
+
+    from apsep_gb300 import Plan, consumers
+
+    n = 1 << 25
+    g = torch.Generator(device=dev)
+    g.manual_seed(31)
+    x = torch.randint(-(1 << 31), 1 << 31, (n,), generator=g, device=dev, dtype=torch.int64).to(torch.int32)
+    h = torch.randint(0, 1 << 20, (n,), generator=g, device=dev, dtype=torch.int32)
+    plan = Plan(n, torch.int32, device=dev)
+    work = torch.empty(consumers.workspace_bytes(n), dtype=torch.uint8, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ops = {  # name: (call, caller bytes per key, pass bytes per key)
+        "prev_greater": (lambda: consumers.prev_greater(x, plan=plan, work=work), 8, 16),
+        "next_smaller": (lambda: consumers.next_smaller(x, plan=plan, work=work), 8, 24),
+        "stock_span": (lambda: consumers.stock_span(x, plan=plan, work=work), 8, 24),
+        "cartesian_parents": (lambda: consumers.cartesian_parents(x, plan=plan, work=work), 8, 40),
+        "largest_rectangle": (lambda: consumers.largest_rectangle(h, plan=plan, work=work), 4, 36),
+    }
+    res = {}
+    for name, (call, ub, pb) in ops.items():
+        for _ in range(3):
+            call()
+        ts = []
+        for _ in range(7):
+            flush_l2(flush)
+            e0.record()
+            call()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
+        ms = statistics.median(ts)
+        res[name] = {"us": round(ms * 1e3, 1), "useful_gbs": round(ub * n / ms / 1e6, 1),
+                     "pass_bytes_per_key": pb, "pass_gbs": round(pb * n / ms / 1e6, 1),
+                     "frac": round(pb * n / ms / 1e6 / peak_gbs, 4)}
+    plan.check()
+    plan.close()
+    return {"workload": "consumers_2p25_int32", "n": n, "ops": res,
+            "note": "largest_rectangle returns one int64 (its time includes the read back)"}
 
 
 def run_served(dev) -> dict:
@@ -567,6 +617,8 @@ def run_ours(args) -> None:
         line["batched"] = run_batched(dev)
         torch.cuda.empty_cache()
         line["served"] = run_served(dev)
+        torch.cuda.empty_cache()
+        line["consumers"] = run_consumers(dev, peaks["hbm_gbs"])
         torch.cuda.empty_cache()
         line["sweep"] = run_sweep(dev, peaks["hbm_gbs"])
     print(json.dumps(line), flush=True)
