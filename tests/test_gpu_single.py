@@ -216,6 +216,36 @@ def test_full_size_2_25(plans, name):
     assert np.array_equal(got, oracle.apse(a))
 
 
+def test_maximum_size_closed_forms():
+    """n = APSEP_MAX_KEYS (2^31 - 4096, the largest n whose tile ends stay in
+    int32): ascending keys answer i - 1, descending keys -1, checked on the
+    device (the arrays hold 8.6 GB each); then the same n behind a 1-key view
+    head (off a 16-byte boundary)."""
+    n = _lib.MAX_KEYS
+    with Plan(n, torch.int32) as plan:
+        x = torch.arange(n, dtype=torch.int32, device="cuda")
+        out = torch.empty(n + 1, dtype=torch.int32, device="cuda")
+        plan.run(x, out=out[:n])
+        plan.check()
+        assert int(out[0]) == -1
+        assert bool((out[1:n] == x[:n - 1]).all())
+        del x
+        torch.cuda.empty_cache()
+        xd = torch.arange(n, 0, -1, dtype=torch.int32, device="cuda")
+        plan.run(xd, out=out[:n])
+        plan.check()
+        assert bool((out[:n] == -1).all())
+        del xd
+        torch.cuda.empty_cache()
+        xb = torch.empty(n + 1, dtype=torch.int32, device="cuda")
+        torch.arange(n, out=xb[1:])
+        out.fill_(7)
+        plan.run(xb[1:], out=out[1:])
+        plan.check()
+        assert int(out[0]) == 7 and int(out[1]) == -1
+        assert bool((out[2:] == xb[1:n]).all())
+
+
 def test_repeated_runs_reuse_plan(plans):
     # the run-to-run control block (tile counter, epoch) resets itself
     plan = plans[torch.int32]
