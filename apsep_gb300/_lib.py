@@ -43,7 +43,7 @@ NOALLOC_MAX_KEYS = 4194304  # APSEP_NOALLOC_MAX_KEYS in include/apsep.h
 MAX_KEYS = 2147479552  # APSEP_MAX_KEYS in include/apsep.h (2^31 - 4096)
 
 APSEP_OK, APSEP_EINVAL, APSEP_ENOMEM, APSEP_ECUDA, APSEP_ETIMEOUT, APSEP_EINTERNAL, APSEP_ENOTSUP = range(7)
-INT32, FLOAT32 = 0, 1
+INT32, FLOAT32, INT64, FLOAT64 = 0, 1, 2, 3
 LT, LE = 0, 1
 
 

@@ -22,7 +22,9 @@ import torch
 from . import _lib
 from ._lib import ApsepError, PlanInfo  # noqa: F401
 
-_DTYPES = {torch.int32: _lib.INT32, torch.float32: _lib.FLOAT32}
+_DTYPES = {torch.int32: _lib.INT32, torch.float32: _lib.FLOAT32, torch.int64: _lib.INT64,
+           torch.float64: _lib.FLOAT64}
+_WIDE = (torch.int64, torch.float64)  # 8-byte keys: single arrays, one configuration
 
 
 def _stream_handle(device: torch.device, stream=None) -> int:
@@ -39,7 +41,7 @@ class Plan:
         for the table shipped for GB300 when present, or None for the
         plan's fixed configuration (set_config)."""
         if dtype not in _DTYPES:
-            raise TypeError("keys must be torch.int32 or torch.float32, got %s" % dtype)
+            raise TypeError("keys must be torch.int32, float32, int64 or float64, got %s" % dtype)
         self._lib = _lib.load()
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None
                                    else torch.device(device).index or 0)
@@ -47,7 +49,9 @@ class Plan:
         self.inclusive = bool(inclusive)
         self.capacity = int(capacity)
         self._h = ctypes.c_void_p()
-        self._cfg = 0
+        self._cfg = 1 if dtype in _WIDE else 0
+        if dtype in _WIDE:
+            tuning = None  # one configuration for 8-byte keys
         if tuning == "default":
             from . import autotune
             tuning = autotune.load()

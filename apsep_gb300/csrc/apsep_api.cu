@@ -49,16 +49,24 @@ PFN_cuTensorMapEncodeTiled_v12000 encoder() {
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// 2-D view of n keys as rows of 32 (128 bytes), box = one tile.
+bool wide(int dtype) { return dtype == APSEP_INT64 || dtype == APSEP_FLOAT64; }
+int key_bytes(int dtype) { return wide(dtype) ? 8 : 4; }
+
+// 2-D view of an array as 128-byte rows (32 4-byte or 16 8-byte elements),
+// box = one tile (tile_rows rows).
 bool encode_rows(CUtensorMap* map, const void* base, int rows, int tile_rows, int dtype) {
     auto enc = encoder();
     if (!enc) return false;
-    cuuint64_t dims[2] = {32, (cuuint64_t)rows};
+    const cuuint64_t per_row = (cuuint64_t)(128 / key_bytes(dtype));
+    cuuint64_t dims[2] = {per_row, (cuuint64_t)rows};
     cuuint64_t strides[1] = {128};
-    cuuint32_t box[2] = {32, (cuuint32_t)tile_rows};
+    cuuint32_t box[2] = {(cuuint32_t)per_row, (cuuint32_t)tile_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, dtype == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_INT32, 2,
-                     const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    const CUtensorMapDataType t = dtype == APSEP_FLOAT32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                  : dtype == APSEP_INT64   ? CU_TENSOR_MAP_DATA_TYPE_INT64
+                                  : dtype == APSEP_FLOAT64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                                           : CU_TENSOR_MAP_DATA_TYPE_INT32;
+    CUresult r = enc(map, t, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
@@ -116,7 +124,7 @@ apsep_status apsep_config_shape(int32_t config, int32_t* threads, int32_t* keys_
 apsep_status apsep_plan_create(apsep_plan** out, apsep_dtype dtype, apsep_cmp cmp, int64_t capacity) {
     if (!out) return APSEP_EINVAL;
     *out = nullptr;
-    if ((dtype != APSEP_INT32 && dtype != APSEP_FLOAT32) || (cmp != APSEP_LT && cmp != APSEP_LE))
+    if ((dtype != APSEP_INT32 && dtype != APSEP_FLOAT32 && !wide(dtype)) || (cmp != APSEP_LT && cmp != APSEP_LE))
         return APSEP_EINVAL;
     // int32 positions; the last tile's end (up to n rounded up to whole tiles)
     // must stay below 2^31 as well
@@ -132,14 +140,15 @@ apsep_status apsep_plan_create(apsep_plan** out, apsep_dtype dtype, apsep_cmp cm
     p->dtype = dtype;
     p->cmp = cmp;
     p->capacity = capacity;
-    const size_t total = carve_scratch(nullptr, capacity, nullptr);
+    p->cfg = wide(dtype) ? 1 : 0;  // 8-byte keys: the one configuration their kernels have (8 keys per lane)
+    const size_t total = carve_scratch(nullptr, capacity, nullptr, key_bytes(dtype));
     if (cudaMalloc(&p->scratch, total) != cudaSuccess) {
         cudaGetLastError();
         delete p;
         return APSEP_ENOMEM;
     }
     p->scratch_bytes = total;
-    carve_scratch(p->scratch, capacity, &p->rs);
+    carve_scratch(p->scratch, capacity, &p->rs, key_bytes(dtype));
     Counters c0;
     memset(&c0, 0, sizeof(c0));
     c0.epoch = 1;
@@ -151,7 +160,7 @@ apsep_status apsep_plan_create(apsep_plan** out, apsep_dtype dtype, apsep_cmp cm
         return APSEP_ECUDA;
     }
     for (int cfg = 0; cfg < kNumTileConfigs; cfg++)
-        if (range_prepare(cfg) != cudaSuccess) {
+        if (range_prepare(cfg) != cudaSuccess || (wide(dtype) && prepare_wide() != cudaSuccess)) {
             cudaGetLastError();
             cudaFree(p->scratch);
             delete p;
@@ -184,6 +193,7 @@ apsep_status apsep_plan_get_info(const apsep_plan* p, apsep_plan_info* info) {
 
 apsep_status apsep_plan_set_config(apsep_plan* p, int32_t config) {
     if (!p || config < 0 || config >= kNumTileConfigs) return APSEP_EINVAL;
+    if (wide(p->dtype) && config != 1) return APSEP_ENOTSUP;  // 8-byte keys: 8 keys per lane only
     p->cfg = config;
     return APSEP_OK;
 }
@@ -200,13 +210,46 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
     if (offsets && (nseg < 1 || (uintptr_t)offsets % 8 != 0)) return APSEP_EINVAL;
     if (n == 0) return APSEP_OK;
     if (n > p->capacity || !d_in || !d_out) return APSEP_EINVAL;
-    if ((uintptr_t)d_in % 4 != 0 || (uintptr_t)d_out % 4 != 0) return APSEP_EINVAL;  // 4-byte keys and answers
-    if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_EINVAL;
+    const size_t kb = (size_t)key_bytes(p->dtype);
+    if ((uintptr_t)d_in % kb != 0 || (uintptr_t)d_out % 4 != 0) return APSEP_EINVAL;  // keys, answers aligned
+    if (ranges_overlap(d_in, (size_t)n * kb, d_out, (size_t)n * 4)) return APSEP_EINVAL;
     if (offsets && (ranges_overlap(offsets, (size_t)(nseg + 1) * 8, d_out, (size_t)n * 4) ||
-                    ranges_overlap(offsets, (size_t)(nseg + 1) * 8, d_in, (size_t)n * 4)))
+                    ranges_overlap(offsets, (size_t)(nseg + 1) * 8, d_in, (size_t)n * kb)))
         return APSEP_EINVAL;
     DeviceGuard g(p->device);
     if (!g.ok) return APSEP_ECUDA;
+    if (wide(p->dtype)) {  // 8-byte keys: single arrays, TMA when both arrays are 16-byte aligned
+        if (offsets) return APSEP_ENOTSUP;
+        const int B = kWideTileKeys, key_rows_per_tile = B * 8 / 128;
+        int rows = (int)(n / 16);  // 128-byte rows of keys
+        CUtensorMap mi, mo;
+        memset(&mi, 0, sizeof(mi));
+        memset(&mo, 0, sizeof(mo));
+        if ((uintptr_t)d_in % 16 != 0 || (uintptr_t)d_out % 16 != 0 || rows < key_rows_per_tile) rows = 0;
+        if (rows > 0) {
+            if (!encode_rows(&mi, d_in, rows, key_rows_per_tile, p->dtype) ||
+                !encode_rows(&mo, d_out, (int)(n / 32), B / 32, APSEP_INT32))
+                return APSEP_ECUDA;
+        }
+        RangeArgs a;
+        a.d_in = d_in;
+        a.d_out = d_out;
+        a.n = (int)n;
+        a.head = 0;
+        a.num_tiles = (int)((n + B - 1) / B);
+        a.tiles_per_range = 0;
+        a.num_ranges = 0;
+        a.tma_rows = rows;
+        a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
+        a.skip_publish_range = p->dbg_skip_range;
+        a.offsets = nullptr;
+        a.nseg = 0;
+        a.s = p->rs;
+        p->dbg_skip_range = -1;
+        p->dbg_spin_limit = 0;
+        const cudaError_t e = launch_range_wide(p->dtype, cmp == APSEP_LE ? 1 : 0, a, mi, mo, (cudaStream_t)stream);
+        return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
+    }
 
     const TileConfig tc = kTileConfigs[p->cfg];
     const int B = 32 * tc.ipt;  // keys per warp tile

@@ -119,6 +119,7 @@ apsep_status check_args(apsep_plan* plan, const void* d_in, const void* d_out, s
     const apsep_status s = apsep_plan_get_info(plan, &info);
     if (s != APSEP_OK) return s;
     *dtype = info.dtype;
+    if (info.dtype != APSEP_INT32 && info.dtype != APSEP_FLOAT32) return APSEP_ENOTSUP;  // 4-byte keys
     if (n == 0) return APSEP_OK;
     if (n > info.capacity || !d_in || !d_out || !d_work) return APSEP_EINVAL;
     if ((uintptr_t)d_work % 16 != 0 || (uintptr_t)d_in % 4 != 0) return APSEP_EINVAL;

@@ -46,6 +46,21 @@ template <> struct KeyTraits<float> {
     }
 };
 
+// 8-byte keys (int64 / float64, with int32 positions): bits are the raw
+// 64-bit pattern; their status words keep the key apart from the tag.
+template <> struct KeyTraits<int64_t> {
+    __device__ __forceinline__ static int64_t pad() { return LLONG_MAX; }
+    __device__ __forceinline__ static int64_t vmin(int64_t a, int64_t b) { return a < b ? a : b; }
+    __device__ __forceinline__ static uint64_t bits(int64_t a) { return (uint64_t)a; }
+    __device__ __forceinline__ static int64_t from_bits(uint64_t b) { return (int64_t)b; }
+};
+template <> struct KeyTraits<double> {
+    __device__ __forceinline__ static double pad() { return __longlong_as_double(0x7ff0000000000000LL); }  // +inf
+    __device__ __forceinline__ static double vmin(double a, double b) { return fmin(a, b); }
+    __device__ __forceinline__ static uint64_t bits(double a) { return (uint64_t)__double_as_longlong(a); }
+    __device__ __forceinline__ static double from_bits(uint64_t b) { return __longlong_as_double((long long)b); }
+};
+
 // lt(a, b): "a qualifies as the answer for query b".  INCL=false is the
 // strict previous-smaller (APSEP), INCL=true previous-smaller-or-equal; the
 // reference routes every comparison through the same predicate
@@ -62,6 +77,12 @@ __device__ __forceinline__ bool lt(T a, T b) { return INCL ? (a <= b) : (a < b);
 // free.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int swz(int e) { return e ^ ((e >> 3) & 0x1C); }
+// The same map in 8-byte element units: element e -> e ^ ((e>>3)&0x0E)
+// (chunk (e>>1)&7 of row e>>4); pairs stay contiguous.
+__device__ __forceinline__ int swz8(int e) { return e ^ ((e >> 3) & 0x0E); }
+// Swizzled index of key e in a key array of KB-byte keys.
+template <int KB>
+__device__ __forceinline__ int kswz(int e) { return KB == 8 ? swz8(e) : swz(e); }
 
 // ---------------------------------------------------------------------------
 // mbarrier

@@ -40,6 +40,7 @@ struct RangeScratch {
                             //   over each group of 32 ranges; all-ones when created
     uint32_t* cta_ready;    // [kMaxCtas * kReadyStride] epoch in which every range has published, one line per CTA
     uint64_t* range_state;  // [max_ranges] tag<<32 | key bits: min of a finished range
+    uint64_t* range_key;    // [max_ranges] 8-byte keys: the range minimum (range_state holds the tag)
     void* top_key;          // [max_ranges * kTopEntries] key: top of each range's final stack, bottom first
     int32_t* top_pos;       // [max_ranges * kTopEntries] their positions
     uint32_t* top_cnt;      // [max_ranges] entries published | bit 31: they are the whole stack
@@ -60,11 +61,12 @@ constexpr int kTopEntries = 32;           // stack entries each range publishes 
 
 // Byte offsets of the scratch arrays for `capacity` keys (256-byte aligned).
 struct ScratchOffsets {
-    size_t gmin, ready, state, topk, topp, topc, tmin, cmin, flag, mask, total;
+    size_t gmin, ready, state, rkey, topk, topp, topc, tmin, cmin, flag, mask, total;
     int64_t cap_tiles;
 };
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
-constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
+// kb: bytes per key (4: int32 / float32; 8: int64 / float64).
+constexpr ScratchOffsets scratch_offsets(int64_t capacity, int kb = 4) {
     ScratchOffsets o{};
     const int64_t cap = capacity > 0 ? capacity : 1;
     o.cap_tiles = (cap + kMinTileKeys - 1) / kMinTileKeys + 1;
@@ -72,12 +74,13 @@ constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
     o.gmin = align256(sizeof(Counters));
     o.ready = align256(o.gmin + (size_t)(kMaxRanges / 32) * 8);
     o.state = align256(o.ready + (size_t)kMaxCtas * kReadyStride * 4);
-    o.topk = align256(o.state + (size_t)kMaxRanges * 8);
-    o.topp = align256(o.topk + (size_t)kMaxRanges * kTopEntries * 4);
+    o.rkey = align256(o.state + (size_t)kMaxRanges * 8);
+    o.topk = align256(o.rkey + (size_t)kMaxRanges * 8);
+    o.topp = align256(o.topk + (size_t)kMaxRanges * kTopEntries * kb);
     o.topc = align256(o.topp + (size_t)kMaxRanges * kTopEntries * 4);
     o.tmin = align256(o.topc + (size_t)kMaxRanges * 4);
-    o.cmin = align256(o.tmin + (size_t)o.cap_tiles * 4);
-    o.flag = align256(o.cmin + cap_chunks * 4);
+    o.cmin = align256(o.tmin + (size_t)o.cap_tiles * kb);
+    o.flag = align256(o.cmin + cap_chunks * kb);
     o.mask = align256(o.flag + (size_t)o.cap_tiles * 4);
     o.total = align256(o.mask + (size_t)o.cap_tiles * (kMaxTileKeys / 32) * 4);
     return o;
@@ -88,8 +91,8 @@ constexpr ScratchOffsets scratch_offsets(int64_t capacity) {
 constexpr size_t control_bytes() { return sizeof(Counters); }
 constexpr size_t group_min_bytes() { return (size_t)(kMaxRanges / 32) * 8; }
 
-// Bytes of scratch for `capacity` keys; when base != nullptr also fills *s.
-size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s);
+// Bytes of scratch for `capacity` keys of kb bytes; when base != nullptr also fills *s.
+size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s, int kb = 4);
 
 struct RangeArgs {
     const void* d_in;
@@ -136,6 +139,13 @@ cudaError_t range_prepare(int cfg);  // smem attributes + occupancy, current dev
 // each key's segment start.
 cudaError_t launch_range_segmented(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& map_in,
                                    const CUtensorMap& map_out, cudaStream_t stream);
+// 8-byte keys (dtype 2: int64, 3: float64): one configuration (8 keys per
+// lane, 8 warps per CTA), single arrays.
+constexpr int kWideTileKeys = 256;
+cudaError_t prepare_wide();
+cudaError_t launch_range_wide(int dtype, int incl, RangeArgs& a, const CUtensorMap& map_in,
+                              const CUtensorMap& map_out, cudaStream_t st);
+
 // A single array behind a view head (RangeArgs::head > 0): the segmented
 // kernel with one implicit segment and the whole-tile early paths.
 cudaError_t prepare_view(int cfg, int* ctas_per_sm);

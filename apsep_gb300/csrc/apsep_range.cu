@@ -11,14 +11,15 @@ const TileConfig kTileConfigs[kNumTileConfigs] = {
     {8, 8},   // 8 warps per CTA, 256-key warp tiles
 };
 
-size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s) {
-    const ScratchOffsets o = scratch_offsets(capacity);
+size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s, int kb) {
+    const ScratchOffsets o = scratch_offsets(capacity, kb);
     if (base && s) {
         char* b = (char*)base;
         s->ctr = (Counters*)b;
         s->group_min = (uint64_t*)(b + o.gmin);
         s->cta_ready = (uint32_t*)(b + o.ready);
         s->range_state = (uint64_t*)(b + o.state);
+        s->range_key = (uint64_t*)(b + o.rkey);
         s->top_key = b + o.topk;
         s->top_pos = (int32_t*)(b + o.topp);
         s->top_cnt = (uint32_t*)(b + o.topc);

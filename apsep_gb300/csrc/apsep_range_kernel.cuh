@@ -50,29 +50,30 @@ constexpr int kXQueries = 3;    // cross-lane queries per lane and round (32 * 4
 constexpr int kDefCap = 64;     // deferred keys listed in shared memory per range
 constexpr int kCapCap = 16;     // capped keys listed in shared memory per range
 
-// Shared memory of one warp.
-template <int IPT>
+// Shared memory of one warp (KB: bytes per key).
+template <int IPT, int KB = 4>
 struct WLayout {
     static constexpr int WT = 32 * IPT;                              // keys per warp tile
     static constexpr size_t kV = 0;                                   // T[S][WT], swizzled (TMA dst)
-    static constexpr size_t kO = kV + (size_t)kStages * WT * 4;       // int32[WT], swizzled (TMA src)
+    static constexpr size_t kO = kV + (size_t)kStages * WT * KB;      // int32[WT], swizzled (TMA src)
     static constexpr size_t kSM = kO + (size_t)WT * 4;                // T[WT], swizzled: lane suffix minima
-    static constexpr size_t kList = kSM + (size_t)WT * 4;             // int16[WT]: X keys in order
+    static constexpr size_t kList = kSM + (size_t)WT * KB;            // int16[WT]: X keys in order
     static constexpr size_t kStkV = kList + (size_t)WT * 2;           // T[K]
-    static constexpr size_t kStkP = kStkV + (size_t)kStackCap * 4;    // int32[K]
+    static constexpr size_t kStkP = kStkV + (size_t)kStackCap * KB;   // int32[K]
     static constexpr size_t kDefP = kStkP + (size_t)kStackCap * 4;    // int32[kDefCap]
     static constexpr size_t kDefV = kDefP + (size_t)kDefCap * 4;      // T[kDefCap]
-    static constexpr size_t kCapP = kDefV + (size_t)kDefCap * 4;      // int32[kCapCap]
+    static constexpr size_t kCapP = kDefV + (size_t)kDefCap * KB;     // int32[kCapCap]
     static constexpr size_t kCapS = kCapP + (size_t)kCapCap * 4;      // int32[kCapCap]: segment starts
     static constexpr size_t kBar = (kCapS + (size_t)kCapCap * 4 + 7) / 8 * 8;  // uint64[S]
     static constexpr size_t kEnd = kBar + (size_t)kStages * 8;
     static constexpr size_t kBytes = (kEnd + 1023) / 1024 * 1024;     // keeps every warp 1024-aligned
-    static_assert(kO % 1024 == 0 && kSM % 1024 == 0 && (WT * 4) % 1024 == 0,
+    static_assert(kO % 1024 == 0 && kSM % 1024 == 0 && (WT * KB) % 1024 == 0,
                   "swizzled buffers need 1024-byte alignment");
+    static_assert(kStkV % 8 == 0 && kDefV % 8 == 0, "8-byte keys need 8-byte aligned arrays");
 };
 
-template <int IPT, int WPC>
-constexpr size_t kernel_smem_bytes() { return WLayout<IPT>::kBytes * WPC + 1024 + 64; }  // + CTA words
+template <int IPT, int WPC, int KB = 4>
+constexpr size_t kernel_smem_bytes() { return WLayout<IPT, KB>::kBytes * WPC + 1024 + 64; }  // + CTA words
 
 __device__ __forceinline__ uint32_t make_tag(uint32_t epoch, uint32_t flag) { return (epoch << 2) | flag; }
 
@@ -86,6 +87,30 @@ __device__ __forceinline__ T group_key(const uint64_t* w) {
 template <typename T>
 __device__ __forceinline__ T state_key(const uint64_t* w) {
     return KeyTraits<T>::from_bits((uint32_t)__ldcg((const unsigned long long*)w));
+}
+
+// The published minimum of range i (8-byte keys keep it beside the tag word).
+template <typename T>
+__device__ __forceinline__ T range_min(const RangeArgs& a, int i) {
+    if constexpr (sizeof(T) == 8)
+        return KeyTraits<T>::from_bits((uint64_t)__ldcg((const unsigned long long*)&a.s.range_key[i]));
+    else
+        return state_key<T>(&a.s.range_state[i]);
+}
+
+// The minimum of group g (32 ranges), every range of which has published:
+// its atomic word for 4-byte keys, the minimum of its ranges' words for
+// 8-byte keys (no 64-bit key fits beside a tag in one atomic word).
+template <typename T>
+__device__ __forceinline__ T group_min_of(const RangeArgs& a, int g) {
+    if constexpr (sizeof(T) == 8) {
+        T m = KeyTraits<T>::pad();
+        const int e = min(32 * g + 32, a.num_ranges);
+        for (int i = 32 * g; i < e; i++) m = KeyTraits<T>::vmin(m, range_min<T>(a, i));
+        return m;
+    } else {
+        return group_key<T>(&a.s.group_min[g]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -174,13 +199,13 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
         for (int hi = t - 1; hi >= R * tpr && s < 0; hi -= 32) s = ballot_last<T, INCL>(R * tpr, hi, q, tmin);
         if (s < 0) {
             // 4. earlier ranges of the same group, then 5. earlier groups
-            auto rmin = [&](int i) { return state_key<T>(&a.s.range_state[i]); };
+            auto rmin = [&](int i) { return range_min<T>(a, i); };
             const int g = R >> 5;
             int rr = ballot_last<T, INCL>(g * 32, R - 1, q, rmin);
             if (rr < 0) {
                 int gg = -1;
                 for (int hi = g - 1; hi >= 0 && gg < 0; hi -= 32)
-                    gg = ballot_last<T, INCL>(0, hi, q, [&](int i) { return group_key<T>(&a.s.group_min[i]); });
+                    gg = ballot_last<T, INCL>(0, hi, q, [&](int i) { return group_min_of<T>(a, i); });
                 if (gg < 0) return -1;
                 rr = ballot_last<T, INCL>(gg * 32, min(gg * 32 + 31, a.num_ranges - 1), q, rmin);
                 if (rr < 0) return -2;
@@ -203,12 +228,12 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
 template <typename T, bool INCL>
 __device__ __noinline__ int nearest_range(T q, int hi, const RangeArgs& a) {
     if (hi < 0) return -1;
-    auto rmin = [&](int i) { return state_key<T>(&a.s.range_state[i]); };
+    auto rmin = [&](int i) { return range_min<T>(a, i); };
     const int g = hi >> 5;
     const int rr = ballot_last<T, INCL>(g * 32, hi, q, rmin);
     if (rr >= 0) return rr;
     for (int ghi = g - 1; ghi >= 0; ghi -= 32) {
-        const int gg = ballot_last<T, INCL>(0, ghi, q, [&](int i) { return group_key<T>(&a.s.group_min[i]); });
+        const int gg = ballot_last<T, INCL>(0, ghi, q, [&](int i) { return group_min_of<T>(a, i); });
         if (gg >= 0) return ballot_last<T, INCL>(gg * 32, gg * 32 + 31, q, rmin);
     }
     return -1;
@@ -245,11 +270,15 @@ __device__ void range_publish(int r, uint32_t epoch, T rmin, const RangeArgs& a)
     const uint32_t tag = (epoch << 2) | FLAG_AGG;
     int last = 0;
     if (lane == 0 && r != a.skip_publish_range) {
-        red_min_u64(&a.s.group_min[r >> 5], ((uint64_t)(EPOCH_LIMIT - epoch) << 32) | KeyTraits<T>::ord(rmin));
+        if constexpr (sizeof(T) == 8)
+            __stcg((unsigned long long*)&a.s.range_key[r], (unsigned long long)KeyTraits<T>::bits(rmin));
+        else
+            red_min_u64(&a.s.group_min[r >> 5], ((uint64_t)(EPOCH_LIMIT - epoch) << 32) | KeyTraits<T>::ord(rmin));
         // release: this range's words (every lane's, ordered by the caller's
         // __syncwarp) and the group minimum before the range minimum and the count
         __threadfence();
-        __stcg((unsigned long long*)&a.s.range_state[r], ((uint64_t)tag << 32) | KeyTraits<T>::bits(rmin));
+        __stcg((unsigned long long*)&a.s.range_state[r],
+               ((uint64_t)tag << 32) | (sizeof(T) == 8 ? 0u : (uint32_t)KeyTraits<T>::bits(rmin)));
         last = atomicAdd(&a.s.ctr->finished, 1u) == (uint32_t)(a.num_ranges - 1);
         if (last) __threadfence();  // acquire: every range's publication
     }
@@ -276,20 +305,24 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
     // ranges) and the earlier groups, in one round of loads
     auto from_ready = [&]() {
         const int wi = r - 1 - lane;
-        win = wi >= 0 ? state_key<T>(&a.s.range_state[wi]) : KeyTraits<T>::pad();
+        win = wi >= 0 ? range_min<T>(a, wi) : KeyTraits<T>::pad();
         T m = wi >= g * 32 ? win : KeyTraits<T>::pad();
-        const uint32_t gtag = EPOCH_LIMIT - epoch;
-        bool bad = false;
+        if constexpr (sizeof(T) == 8) {  // the ranges of the earlier groups, one by one
+            for (int i = lane; i < g * 32; i += 32) m = KeyTraits<T>::vmin(m, range_min<T>(a, i));
+        } else {
+            const uint32_t gtag = EPOCH_LIMIT - epoch;
+            bool bad = false;
 #pragma unroll
-        for (int k = 0; k < kMaxRanges / 32 / 32; k++) {
-            const int gi = lane + 32 * k;
-            if (gi < g) {
-                const uint64_t w = __ldcg((const unsigned long long*)&a.s.group_min[gi]);
-                bad = bad || (uint32_t)(w >> 32) != gtag;
-                m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_ord((uint32_t)w));
+            for (int k = 0; k < kMaxRanges / 32 / 32; k++) {
+                const int gi = lane + 32 * k;
+                if (gi < g) {
+                    const uint64_t w = __ldcg((const unsigned long long*)&a.s.group_min[gi]);
+                    bad = bad || (uint32_t)(w >> 32) != gtag;
+                    m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_ord((uint32_t)w));
+                }
             }
+            if (bad) atomicOr(&a.s.ctr->err, ERR_INTERNAL);
         }
-        if (bad) atomicOr(&a.s.ctr->err, ERR_INTERNAL);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
         p = m;
@@ -319,14 +352,14 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
         for (int ri = lane; ri < r; ri += 32) {
             const uint64_t w = ld_acquire_u64(&a.s.range_state[ri]);
             if ((uint32_t)(w >> 32) != tag) ok = false;
-            m = KeyTraits<T>::vmin(m, KeyTraits<T>::from_bits((uint32_t)w));
+            m = KeyTraits<T>::vmin(m, sizeof(T) == 8 ? range_min<T>(a, ri) : KeyTraits<T>::from_bits((uint32_t)w));
         }
         if (__all_sync(FULL, ok)) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
             p = m;
             const int wi = r - 1 - lane;
-            win = wi >= 0 ? state_key<T>(&a.s.range_state[wi]) : KeyTraits<T>::pad();
+            win = wi >= 0 ? range_min<T>(a, wi) : KeyTraits<T>::pad();
             return;
         }
         if (__shfl_sync(FULL, lane == 0 ? (int)(ld_acquire_u32(flag) == epoch) : 0, 0)) {
@@ -343,16 +376,20 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
 }
 
 template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
-__global__ void __launch_bounds__(WPC * 32, (IPT >= 16 ? (WPC >= 16 ? 1 : 2) : 3))
+__global__ void __launch_bounds__(WPC * 32, (sizeof(T) == 8 ? 2 : IPT >= 16 ? (WPC >= 16 ? 1 : 2) : 3))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
-    using L = WLayout<IPT>;
+    constexpr int KB = (int)sizeof(T);  // bytes per key
+    using L = WLayout<IPT, KB>;
     constexpr int WT = L::WT;      // keys per warp tile
-    constexpr int W = WT / 32;     // 32-key chunks (and TMA rows) per warp tile
+    constexpr int W = WT / 32;     // 32-key chunks (and answer TMA rows) per warp tile
+    constexpr int RPT = W * KB / 4;  // key TMA rows (128 bytes) per warp tile
+    static_assert(KB == 4 || (KB == 8 && IPT == 8), "8-byte keys run with 8 keys per lane");
     constexpr int TPC = 32 / IPT;  // lanes per chunk
     constexpr int K = kStackCap;
     constexpr int MW = kMaxTileKeys / 32;  // flag-mask words per tile in global
     static_assert(IPT == 8 || IPT == 16, "IPT must be 8 or 16");
+    auto ks = [](int e) { return kswz<KB>(e); };  // swizzled index of key e in V / sSM
     static_assert((K & (K - 1)) == 0, "the stack ring needs a power-of-two size");
     static_assert(K % 32 == 0 && K <= WT, "a whole-tile push copies the tile's last K keys, 32 per step");
     constexpr unsigned FULL = 0xffffffffu;
@@ -412,12 +449,12 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         const int t0 = r * a.tiles_per_range;
         const int t1 = min(t0 + a.tiles_per_range, a.num_tiles);
         const int ntr = t1 - t0;
-        auto tile_full = [&](int t) { return a.tma_rows > 0 && (t + 1) * W <= a.tma_rows && (t > 0 || head == 0); };
+        auto tile_full = [&](int t) { return a.tma_rows > 0 && (t + 1) * RPT <= a.tma_rows && (t > 0 || head == 0); };
         if (lane == 0) {
             for (int i = 0; i < kStages && i < ntr; i++)
                 if (tile_full(t0 + i)) {
-                    mbar_arrive_expect_tx(&bar[i], (uint32_t)(WT * 4));
-                    tma_load_2d(sV + (size_t)i * WT, &map_in, 0, (t0 + i) * W, &bar[i]);
+                    mbar_arrive_expect_tx(&bar[i], (uint32_t)(WT * KB));
+                    tma_load_2d(sV + (size_t)i * WT, &map_in, 0, (t0 + i) * RPT, &bar[i]);
                 }
         }
         // Range state (warp-uniform): the stack ring [stk_lo, stk_hi) of strict
@@ -461,7 +498,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 for (int j = 0; j < IPT; j++) {
                     const int e = j * 32 + lane;
                     const int g = tile_base + e;
-                    V[swz(e)] = g < a.n && (!head || g >= head) ? d_in[g] : KeyTraits<T>::pad();
+                    V[ks(e)] = g < a.n && (!head || g >= head) ? d_in[g] : KeyTraits<T>::pad();
                 }
                 // A view head makes tile 0 plain while tile kStages streams into its
                 // slot: the plain tile completes the slot barrier's phase by itself.
@@ -516,13 +553,22 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 
             // ---- 1. in-thread answers: compare ladder over IPT keys in registers --------
             T v[IPT];
+            if constexpr (KB == 4) {
 #pragma unroll
-            for (int q4 = 0; q4 < IPT / 4; q4++) {
-                const uint4 rr = *reinterpret_cast<const uint4*>(&V[swz(lane * IPT + 4 * q4)]);
-                v[4 * q4 + 0] = KeyTraits<T>::from_bits(rr.x);
-                v[4 * q4 + 1] = KeyTraits<T>::from_bits(rr.y);
-                v[4 * q4 + 2] = KeyTraits<T>::from_bits(rr.z);
-                v[4 * q4 + 3] = KeyTraits<T>::from_bits(rr.w);
+                for (int q4 = 0; q4 < IPT / 4; q4++) {
+                    const uint4 rr = *reinterpret_cast<const uint4*>(&V[swz(lane * IPT + 4 * q4)]);
+                    v[4 * q4 + 0] = KeyTraits<T>::from_bits(rr.x);
+                    v[4 * q4 + 1] = KeyTraits<T>::from_bits(rr.y);
+                    v[4 * q4 + 2] = KeyTraits<T>::from_bits(rr.z);
+                    v[4 * q4 + 3] = KeyTraits<T>::from_bits(rr.w);
+                }
+            } else {  // two 8-byte keys per 16-byte chunk
+#pragma unroll
+                for (int q2 = 0; q2 < IPT / 2; q2++) {
+                    const ulonglong2 rr = *reinterpret_cast<const ulonglong2*>(&V[ks(lane * IPT + 2 * q2)]);
+                    v[2 * q2 + 0] = KeyTraits<T>::from_bits((uint64_t)rr.x);
+                    v[2 * q2 + 1] = KeyTraits<T>::from_bits((uint64_t)rr.y);
+                }
             }
             const int lb = tile_base + lane * IPT;  // position of this lane's first key
             const int nvalid = min(max(a.n - lb, 0), IPT);
@@ -557,7 +603,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     const T tmin = __shfl_sync(FULL, v[IPT - 1], 31);
                     for (int e = lane; e < WT && def_total + e < kDefCap; e += 32) {
                         sDefP[def_total + e] = tile_base + e;
-                        sDefV[def_total + e] = V[swz(e)];
+                        sDefV[def_total + e] = V[ks(e)];
                     }
                     if (lane < W) __stcg(&a.s.tile_mask[(size_t)t * MW + lane], 0xffffffffu);
                     if (lane == 0) {
@@ -586,8 +632,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     has_rmin = true;
                     __syncwarp();
                     if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
-                        mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * 4));
-                        tma_load_2d(V, &map_in, 0, (t + kStages) * W, &bar[slot]);
+                        mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * KB));
+                        tma_load_2d(V, &map_in, 0, (t + kStages) * RPT, &bar[slot]);
                     }
                     continue;
                 }
@@ -632,7 +678,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 #pragma unroll
                     for (int h = 0; h < K / 32; h++) {  // the tile's last K keys, one per lane and step
                         const int e = WT - K + h * 32 + lane;
-                        sStkV[(base_idx + e) & (K - 1)] = V[swz(e)];
+                        sStkV[(base_idx + e) & (K - 1)] = V[ks(e)];
                         sStkP[(base_idx + e) & (K - 1)] = tile_base + e;
                     }
                     stk_hi = base_idx + WT;
@@ -641,8 +687,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     rmin = KeyTraits<T>::vmin(rmin, first);
                     __syncwarp();
                     if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
-                        mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * 4));
-                        tma_load_2d(V, &map_in, 0, (t + kStages) * W, &bar[slot]);
+                        mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * KB));
+                        tma_load_2d(V, &map_in, 0, (t + kStages) * RPT, &bar[slot]);
                     }
                     continue;
                 }
@@ -688,11 +734,19 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 #pragma unroll
                 for (int k = IPT - 2; k >= 0; k--) sfx[k] = KeyTraits<T>::vmin(v[k], sfx[k + 1]);
                 lmin = sfx[0];
+                if constexpr (KB == 4) {
 #pragma unroll
-                for (int q4 = 0; q4 < IPT / 4; q4++)
-                    *reinterpret_cast<uint4*>(&sSM[swz(lane * IPT + 4 * q4)]) =
-                        make_uint4(KeyTraits<T>::bits(sfx[4 * q4]), KeyTraits<T>::bits(sfx[4 * q4 + 1]),
-                                   KeyTraits<T>::bits(sfx[4 * q4 + 2]), KeyTraits<T>::bits(sfx[4 * q4 + 3]));
+                    for (int q4 = 0; q4 < IPT / 4; q4++)
+                        *reinterpret_cast<uint4*>(&sSM[swz(lane * IPT + 4 * q4)]) =
+                            make_uint4(KeyTraits<T>::bits(sfx[4 * q4]), KeyTraits<T>::bits(sfx[4 * q4 + 1]),
+                                       KeyTraits<T>::bits(sfx[4 * q4 + 2]), KeyTraits<T>::bits(sfx[4 * q4 + 3]));
+                } else {
+#pragma unroll
+                    for (int q2 = 0; q2 < IPT / 2; q2++)
+                        *reinterpret_cast<ulonglong2*>(&sSM[ks(lane * IPT + 2 * q2)]) =
+                            make_ulonglong2((unsigned long long)KeyTraits<T>::bits(sfx[2 * q2]),
+                                            (unsigned long long)KeyTraits<T>::bits(sfx[2 * q2 + 1]));
+                }
             }
             {
                 T cmn = lmin;
@@ -756,7 +810,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     int p[NQ];
 #pragma unroll
                     for (int i2 = 0; i2 < NQ; i2++) {
-                        q[i2] = act[i2] ? V[swz(e[i2])] : KeyTraits<T>::pad();
+                        q[i2] = act[i2] ? V[ks(e[i2])] : KeyTraits<T>::pad();
                         p[i2] = act[i2] ? e[i2] / IPT - 1 : 0;
                     }
 #pragma unroll
@@ -781,7 +835,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 #pragma unroll
                     for (int i2 = 0; i2 < NQ; i2++) {
                         pb[i2] = p[i2] * IPT;
-                        px[i2] = (pb[i2] >> 3) & 0x1C;
+                        px[i2] = (pb[i2] >> 3) & (KB == 4 ? 0x1C : 0x0E);
                     }
 #pragma unroll
                     for (int s2 = IPT / 2; s2 > 0; s2 >>= 1) {
@@ -893,7 +947,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     __syncwarp();
                     const bool act = lane < stot;
                     const int e = act ? (int)sList[lane] : 0;
-                    const int ans = search(act ? V[swz(e)] : KeyTraits<T>::pad(), act);
+                    const int ans = search(act ? V[ks(e)] : KeyTraits<T>::pad(), act);
                     if (act) O[swz(e)] = ans >= 0 ? ans : -2;  // -2: a miss, flagged by the key's lane
                     if (__any_sync(FULL, act && ans < 0)) {      // (only once the stack has dropped entries)
                         __syncwarp();
@@ -913,7 +967,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         const bool act = m != 0;
                         const int k = act ? __ffs(m) - 1 : 0;
                         m &= m - 1;
-                        const int ans = search(act ? V[swz(lane * IPT + k)] : KeyTraits<T>::pad(), act);
+                        const int ans = search(act ? V[ks(lane * IPT + k)] : KeyTraits<T>::pad(), act);
                         if (act) {
                             if (ans >= 0) O[swz(lane * IPT + k)] = ans;
                             else cm |= 1u << k;
@@ -942,7 +996,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             const int k = __ffs(m) - 1;
                             m &= m - 1;
                             sDefP[idx] = lb + k;
-                            sDefV[idx] = V[swz(lane * IPT + k)];
+                            sDefV[idx] = V[ks(lane * IPT + k)];
                             idx++;
                         }
                     }
@@ -1043,7 +1097,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         const int k = __ffs(m) - 1;
                         m &= m - 1;
                         if (idx >= newtop - K) {
-                            sStkV[idx & (K - 1)] = V[swz(lane * IPT + k)];
+                            sStkV[idx & (K - 1)] = V[ks(lane * IPT + k)];
                             sStkP[idx & (K - 1)] = lb + k;
                         }
                         idx++;
@@ -1062,8 +1116,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             has_rmin = true;
             __syncwarp();
             if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
-                mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * 4));
-                tma_load_2d(V, &map_in, 0, (t + kStages) * W, &bar[slot]);
+                mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * KB));
+                tma_load_2d(V, &map_in, 0, (t + kStages) * RPT, &bar[slot]);
             }
         }
 
@@ -1133,19 +1187,36 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 const int cnt = (int)(__ldcg(&a.s.top_cnt[rp]) & 0xffu);
                 const uint4* tk = reinterpret_cast<const uint4*>((const T*)a.s.top_key + (size_t)rp * kTopEntries);
                 const uint4* tp = reinterpret_cast<const uint4*>(a.s.top_pos + (size_t)rp * kTopEntries);
-                uint4 tw[kTopEntries / 4], pw[kTopEntries / 4];
+                if constexpr (KB == 4) {
+                    uint4 tw[kTopEntries / 4], pw[kTopEntries / 4];
 #pragma unroll
-                for (int k = 0; k < kTopEntries / 4; k++) {
-                    tw[k] = __ldcg(&tk[k]);
-                    pw[k] = __ldcg(&tp[k]);
-                }
+                    for (int k = 0; k < kTopEntries / 4; k++) {
+                        tw[k] = __ldcg(&tk[k]);
+                        pw[k] = __ldcg(&tp[k]);
+                    }
 #pragma unroll
-                for (int k = 0; k < kTopEntries / 4; k++) {
-                    const uint32_t wb[4] = {tw[k].x, tw[k].y, tw[k].z, tw[k].w};
-                    const int pb[4] = {(int)pw[k].x, (int)pw[k].y, (int)pw[k].z, (int)pw[k].w};
+                    for (int k = 0; k < kTopEntries / 4; k++) {
+                        const uint32_t wb[4] = {tw[k].x, tw[k].y, tw[k].z, tw[k].w};
+                        const int pb[4] = {(int)pw[k].x, (int)pw[k].y, (int)pw[k].z, (int)pw[k].w};
 #pragma unroll
-                    for (int c = 0; c < 4; c++)
-                        if (4 * k + c < cnt && lt<INCL>(KeyTraits<T>::from_bits(wb[c]), q)) ans = pb[c];
+                        for (int c = 0; c < 4; c++)
+                            if (4 * k + c < cnt && lt<INCL>(KeyTraits<T>::from_bits(wb[c]), q)) ans = pb[c];
+                    }
+                } else {  // two 8-byte keys per 16-byte load
+                    uint4 tw[kTopEntries / 2], pw[kTopEntries / 4];
+#pragma unroll
+                    for (int k = 0; k < kTopEntries / 2; k++) tw[k] = __ldcg(&tk[k]);
+#pragma unroll
+                    for (int k = 0; k < kTopEntries / 4; k++) pw[k] = __ldcg(&tp[k]);
+#pragma unroll
+                    for (int k = 0; k < kTopEntries / 2; k++) {
+                        const uint64_t kb2[2] = {((uint64_t)tw[k].y << 32) | tw[k].x, ((uint64_t)tw[k].w << 32) | tw[k].z};
+                        const uint4 p4 = pw[k / 2];
+                        const int pb2[2] = {(int)(k % 2 ? p4.z : p4.x), (int)(k % 2 ? p4.w : p4.y)};
+#pragma unroll
+                        for (int c = 0; c < 2; c++)
+                            if (2 * k + c < cnt && lt<INCL>(KeyTraits<T>::from_bits(kb2[c]), q)) ans = pb2[c];
+                    }
                 }
             }
             unsigned fb = __ballot_sync(FULL, want && ans == -2);
@@ -1294,7 +1365,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
 inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo, cudaStream_t st,
                             int max_warps) {
-    constexpr size_t smem = kernel_smem_bytes<IPT, WPC>();
+    constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
     int tpr = (a.num_tiles + max_warps - 1) / max_warps;
     if (tpr < 1) tpr = 1;
     a.tiles_per_range = tpr;
@@ -1306,7 +1377,7 @@ inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorM
 
 template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
 inline cudaError_t prepare_t(int* ctas_per_sm) {
-    constexpr size_t smem = kernel_smem_bytes<IPT, WPC>();
+    constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
     auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

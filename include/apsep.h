@@ -3,8 +3,9 @@
  *
  * All Previous Smaller Element: for each key a[i], out[i] is the largest
  * j < i with a[j] < a[i] (APSEP_LT) or a[j] <= a[i] (APSEP_LE), else -1.
- * Keys are int32 or float32 (finite: NaN keys are outside the contract),
- * outputs are int32 indices, so n <= APSEP_MAX_KEYS = 2^31 - 4096.
+ * Keys are int32, float32, int64 or float64 (finite: NaN keys are outside
+ * the contract), outputs are int32 indices, so n <= APSEP_MAX_KEYS =
+ * 2^31 - 4096.
  *
  * Plain pointers and sizes only: device pointers from any allocator
  * (cudaMalloc, torch), `stream` is a cudaStream_t passed as void* (NULL = the
@@ -48,7 +49,12 @@ typedef enum apsep_status {
     APSEP_ENOTSUP = 6    /* unsupported dtype / device */
 } apsep_status;
 
-typedef enum apsep_dtype { APSEP_INT32 = 0, APSEP_FLOAT32 = 1 } apsep_dtype;
+/* Key types.  8-byte keys (the reference's ApsepInfinity<long long/double>,
+ * src/apsep.cuh:62-70) keep int32 positions (n <= APSEP_MAX_KEYS) and run
+ * single arrays only: apsep_run_segmented, apsep_run_noalloc and the
+ * consumers return APSEP_ENOTSUP / APSEP_EINVAL for them, and their plans
+ * have one configuration (1). */
+typedef enum apsep_dtype { APSEP_INT32 = 0, APSEP_FLOAT32 = 1, APSEP_INT64 = 2, APSEP_FLOAT64 = 3 } apsep_dtype;
 
 typedef enum apsep_cmp {
     APSEP_LT = 0, /* strict previous-smaller (the reference's INCL=false) */

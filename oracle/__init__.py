@@ -51,7 +51,7 @@ def _load():
     if _lib is None:
         lib = ctypes.CDLL(build())
         i64, i32, vp = ctypes.c_int64, ctypes.c_int, ctypes.c_void_p
-        for name in ("oracle_apse_i32", "oracle_apse_f32"):
+        for name in ("oracle_apse_i32", "oracle_apse_f32", "oracle_apse_i64", "oracle_apse_f64"):
             f = getattr(lib, name)
             f.argtypes = [vp, i64, i32, vp]
             f.restype = i32
@@ -69,7 +69,11 @@ def _fn(a: np.ndarray, seg: bool):
         return lib.oracle_apse_segmented_i32 if seg else lib.oracle_apse_i32
     if a.dtype == np.float32:
         return lib.oracle_apse_segmented_f32 if seg else lib.oracle_apse_f32
-    raise TypeError("oracle supports int32 and float32 keys, got %s" % a.dtype)
+    if a.dtype == np.int64 and not seg:
+        return lib.oracle_apse_i64
+    if a.dtype == np.float64 and not seg:
+        return lib.oracle_apse_f64
+    raise TypeError("oracle supports int32 / float32 keys (and int64 / float64 single arrays), got %s" % a.dtype)
 
 
 def apse(a: np.ndarray, le: bool = False) -> np.ndarray:

@@ -16,7 +16,7 @@
  * "!(a[top] < a[i])" equals cpuApsep's "a[top] >= a[i]" for integers and for
  * finite floats, so one routine covers both.
  *
- * Generic over the key type (int32, float32) through a macro, plus a
+ * Generic over the key type (int32, float32, int64, float64) through a macro, plus a
  * segmented form (answers relative to each segment's start, never crossing a
  * segment's left edge) for the batched API.
  *
@@ -54,6 +54,18 @@ int oracle_apse_i32(const int32_t* a, int64_t n, int le, int32_t* out) {
 int oracle_apse_f32(const float* a, int64_t n, int le, int32_t* out) {
     if (n < 0 || n > INT32_MAX) return -2;
     APSE_BODY(float)
+}
+
+/* 8-byte keys (the reference's ApsepInfinity<long long / double>,
+ * src/apsep.cuh:62-70): the same stack, int32 positions. */
+int oracle_apse_i64(const int64_t* a, int64_t n, int le, int32_t* out) {
+    if (n < 0 || n > INT32_MAX) return -2;
+    APSE_BODY(int64_t)
+}
+
+int oracle_apse_f64(const double* a, int64_t n, int le, int32_t* out) {
+    if (n < 0 || n > INT32_MAX) return -2;
+    APSE_BODY(double)
 }
 
 /* Segmented form: segment s covers [offsets[s], offsets[s+1]); each answer is

@@ -98,3 +98,15 @@ def test_oracle_matches_reference_binary_random():
         d = rng.integers(0, 4, n).astype(np.int32)
         assert np.array_equal(oracle.apse(d, False), oracle.ref_apse(d, False))
         assert np.array_equal(oracle.apse(d, True), oracle.ref_apse(d, True))
+
+
+def test_oracle_eight_byte_keys():
+    """int64 / float64 keys: the monotone stack against a direct scan."""
+    rng = np.random.default_rng(64)
+    for a in (rng.integers(-(1 << 62), 1 << 62, 700, dtype=np.int64),
+              (np.int64(1) << 40) + rng.integers(0, 4, 700, dtype=np.int64),
+              1.0 + rng.integers(0, 5, 700) * 2.0 ** -40):
+        for le in (False, True):
+            want = np.array([max([j for j in range(i) if (a[j] <= a[i] if le else a[j] < a[i])], default=-1)
+                             for i in range(len(a))], dtype=np.int32)
+            assert np.array_equal(oracle.apse(a, le), want)
