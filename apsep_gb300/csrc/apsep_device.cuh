@@ -61,6 +61,19 @@ template <> struct KeyTraits<double> {
     __device__ __forceinline__ static double from_bits(uint64_t b) { return __longlong_as_double((long long)b); }
 };
 
+// float64 keys compare as int64 (the FP64 pipe is slow on this part): the
+// order-preserving map of a float64 bit pattern to int64, both zeros to 0,
+// so a < b as doubles <=> f64_order(a) < f64_order(b) for every non-NaN pair.
+__device__ __forceinline__ int64_t f64_order(int64_t b) {
+    return (b << 1) == 0 ? 0 : (b ^ ((b >> 63) & 0x7fffffffffffffffLL));
+}
+// A key from global memory, mapped when MAPF (int64 slots holding float64 bits).
+template <typename T, bool MAPF>
+__device__ __forceinline__ T load_key(const T* p) {
+    if constexpr (MAPF) return (T)f64_order((int64_t)__ldg(p));
+    else return __ldg(p);
+}
+
 // lt(a, b): "a qualifies as the answer for query b".  INCL=false is the
 // strict previous-smaller (APSEP), INCL=true previous-smaller-or-equal; the
 // reference routes every comparison through the same predicate

@@ -170,7 +170,7 @@ static __device__ __noinline__ int seg_find(const int64_t* __restrict__ off, int
 // Answer relative to the segment start s: an answer before the segment is none.
 __device__ __forceinline__ int seg_rel(int g, int s) { return g >= s ? g - s : -1; }
 
-template <typename T, int B, bool INCL>
+template <typename T, int B, bool INCL, bool MAPF = false>
 __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in, const T* __restrict__ tile_min,
                                       const T* __restrict__ chunk_min, const RangeArgs& a) {
     constexpr int W = B / 32;
@@ -183,7 +183,7 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
     {  // 1. the row holding limit-1, positions below limit
         const int row = t * B + c * 32;
         const int p = row + lane;
-        const bool ok = p < limit && p >= a.head && lt<INCL>(__ldg(&d_in[p]), q);
+        const bool ok = p < limit && p >= a.head && lt<INCL>(load_key<T, MAPF>(&d_in[p]), q);
         const unsigned m = __ballot_sync(0xffffffffu, ok);
         if (m) return row + 31 - __clz(m);
     }
@@ -218,7 +218,8 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
         if (cc < 0) return -2;
     }
     const int row = s * B + cc * 32;
-    const unsigned m = __ballot_sync(0xffffffffu, row + lane >= a.head && lt<INCL>(__ldg(&d_in[row + lane]), q));
+    const unsigned m =
+        __ballot_sync(0xffffffffu, row + lane >= a.head && lt<INCL>(load_key<T, MAPF>(&d_in[row + lane]), q));
     return m ? row + 31 - __clz(m) : -2;
 }
 
@@ -375,7 +376,9 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
     }
 }
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
+// MAPF: int64 key slots that hold float64 bit patterns, compared through
+// f64_order (keys are mapped as they enter shared memory or registers).
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false>
 __global__ void __launch_bounds__(WPC * 32, (sizeof(T) == 8 ? 2 : IPT >= 16 ? (WPC >= 16 ? 1 : 2) : 3))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
@@ -493,12 +496,20 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 
             if (full) {
                 if (!mbar_wait_bounded(&bar[slot], par, a.spin_limit) && lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+                if constexpr (MAPF) {  // the tile's float64 bits become ordered int64 keys, in place
+#pragma unroll
+                    for (int j = 0; j < IPT; j++) {
+                        const int e = j * 32 + lane;
+                        V[ks(e)] = (T)f64_order((int64_t)V[ks(e)]);
+                    }
+                }
             } else {
 #pragma unroll
                 for (int j = 0; j < IPT; j++) {
                     const int e = j * 32 + lane;
                     const int g = tile_base + e;
-                    V[ks(e)] = g < a.n && (!head || g >= head) ? d_in[g] : KeyTraits<T>::pad();
+                    V[ks(e)] = g < a.n && (!head || g >= head) ? (MAPF ? load_key<T, MAPF>(&d_in[g]) : d_in[g])
+                                                                : KeyTraits<T>::pad();
                 }
                 // A view head makes tile 0 plain while tile kStages streams into its
                 // slot: the plain tile completes the slot barrier's phase by itself.
@@ -1226,7 +1237,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 const T qf = __shfl_sync(FULL, q, f);
                 const int rpf = __shfl_sync(FULL, rp, f);
                 const int lim = rpf >= 0 ? range_end(rpf) : range_begin;
-                const int found = find_left<T, WT, INCL>(qf, lim, d_in, tile_min_r, chunk_min_r, a);
+                const int found = find_left<T, WT, INCL, MAPF>(qf, lim, d_in, tile_min_r, chunk_min_r, a);
                 if (lane == f) ans = found;
             }
             if (want) {
@@ -1250,13 +1261,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     const int pos = t * WT + w * 32 + lane;
                     unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from && (!head || pos >= head));
                     if (!pend) continue;
-                    const T q = ((pend >> lane) & 1u) ? __ldg(&d_in[pos]) : KeyTraits<T>::pad();
+                    const T q = ((pend >> lane) & 1u) ? load_key<T, MAPF>(&d_in[pos]) : KeyTraits<T>::pad();
                     if (mixed) {  // deferred and capped keys: a full search each
                         while (pend) {
                             const int f = __ffs(pend) - 1;
                             pend &= pend - 1;
                             const int pf = t * WT + w * 32 + f;
-                            const int found = find_left<T, WT, INCL>(__shfl_sync(FULL, q, f), pf, d_in, tile_min_r,
+                            const int found = find_left<T, WT, INCL, MAPF>(__shfl_sync(FULL, q, f), pf, d_in, tile_min_r,
                                                                      chunk_min_r, a);
                             int sf = 0;
                             if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
@@ -1283,7 +1294,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         if (!pend) break;
                         const int f = __ffs(pend) - 1;
                         const T qf = __shfl_sync(FULL, q, f);
-                        const int found = find_left<T, WT, INCL>(qf, cur >= 0 ? cur : range_begin, d_in, tile_min_r,
+                        const int found = find_left<T, WT, INCL, MAPF>(qf, cur >= 0 ? cur : range_begin, d_in, tile_min_r,
                                                                  chunk_min_r, a);
                         if (found < 0) {
                             if (lane == 0) atomicOr(err, ERR_INTERNAL);
@@ -1291,7 +1302,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             a_done = true;
                         } else {
                             cur = found;
-                            cv = __ldg(&d_in[cur]);
+                            cv = load_key<T, MAPF>(&d_in[cur]);
                         }
                     }
                 }
@@ -1302,7 +1313,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         const int ncap = min(cap_total, kCapCap);
         for (int j = 0; j < ncap; j++) {
             const int pos = sCapP[j];
-            const int found = find_left<T, WT, INCL>(__ldg(&d_in[pos]), pos, d_in, tile_min_r, chunk_min_r, a);
+            const int found = find_left<T, WT, INCL, MAPF>(load_key<T, MAPF>(&d_in[pos]), pos, d_in, tile_min_r,
+                                                           chunk_min_r, a);
             if (lane == 0) {
                 if (found < 0) atomicOr(err, ERR_INTERNAL);
                 else if (!head || pos >= head) a.d_out[pos] = SEG ? seg_rel(found, sCapS[j]) : found;
@@ -1323,7 +1335,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         pend &= pend - 1;
                         const int pf = t * WT + w * 32 + f;
                         const int found =
-                            find_left<T, WT, INCL>(__ldg(&d_in[pf]), pf, d_in, tile_min_r, chunk_min_r, a);
+                            find_left<T, WT, INCL, MAPF>(load_key<T, MAPF>(&d_in[pf]), pf, d_in, tile_min_r, chunk_min_r, a);
                         int sf = 0;
                         if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
                         if (lane == f) {
@@ -1362,7 +1374,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 // ---------------------------------------------------------------------------
 // Launch plumbing shared by the single-array and segmented translation units.
 // ---------------------------------------------------------------------------
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false>
 inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo, cudaStream_t st,
                             int max_warps) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
@@ -1371,14 +1383,14 @@ inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorM
     a.tiles_per_range = tpr;
     a.num_ranges = (a.num_tiles + tpr - 1) / tpr;
     const int ctas = (a.num_ranges + WPC - 1) / WPC;
-    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
+    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
     return cudaGetLastError();
 }
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false>
 inline cudaError_t prepare_t(int* ctas_per_sm) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
-    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP>;
+    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int n = 0;

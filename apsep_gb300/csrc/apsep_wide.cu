@@ -5,6 +5,9 @@
 // 128-byte TMA rows of 16 keys, answers as int32 positions (n < 2^31).
 // Range minima sit beside their tag words (no 64-bit key fits beside a tag
 // in one atomic word), and group minima are read from the ranges' words.
+// float64 keys run as int64 through an order-preserving map of their bits
+// (applied as keys enter shared memory or registers): the FP64 compare rate
+// of this part would make every comparison the bottleneck.
 // Single arrays only: one configuration, no segmented form, no view head
 // (arrays off a 16-byte boundary take plain loads and stores).
 #include "apsep_range_kernel.cuh"
@@ -27,8 +30,8 @@ cudaError_t prepare_wide() {
     int per_sm = 0;
     cudaError_t rr[4] = {prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true>(&per_sm),
                          prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true>(&per_sm),
-                         prepare_t<double, kWideIpt, kWideWpc, false, false, true>(&per_sm),
-                         prepare_t<double, kWideIpt, kWideWpc, true, false, true>(&per_sm)};
+                         prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true, true>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true, true>(&per_sm)};
     for (int q = 0; q < 4; q++)
         if (rr[q] != cudaSuccess) return rr[q];
     int sms = 0;
@@ -54,8 +57,9 @@ cudaError_t launch_range_wide(int dtype, int incl, RangeArgs& a, const CUtensorM
     if (dtype == 2)
         return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, false, true>(a, mi, mo, st, max_warps)
                     : launch_t<int64_t, kWideIpt, kWideWpc, false, false, true>(a, mi, mo, st, max_warps);
-    return incl ? launch_t<double, kWideIpt, kWideWpc, true, false, true>(a, mi, mo, st, max_warps)
-                : launch_t<double, kWideIpt, kWideWpc, false, false, true>(a, mi, mo, st, max_warps);
+    // float64: int64 slots compared through the order map (no FP64 compares)
+    return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, false, true, true>(a, mi, mo, st, max_warps)
+                : launch_t<int64_t, kWideIpt, kWideWpc, false, false, true, true>(a, mi, mo, st, max_warps);
 }
 
 }  // namespace apsep

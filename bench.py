@@ -49,6 +49,8 @@ Extra objects on the same line (one GPU only; --no-extras skips them):
   consumers  previous greater, next smaller, stock span, Cartesian parents and
              largest rectangle at N = 2^25 (apsep_gb300.consumers): time,
              useful GB/s and the fraction of peak of all their HBM passes.
+  wide       8-byte keys (int64 / float64) at N = 2^25: time, useful GB/s
+             (12 B/key) and fraction of peak.
   sweep      single-array useful GB/s and roofline fraction for N = 2^14 ..
              2^30 (every second power of two), uniform and descending keys.
 
@@ -323,6 +325,49 @@ def run_consumers(dev, peak_gbs: float) -> dict:
     plan.close()
     return {"workload": "consumers_2p25_int32", "n": n, "ops": res,
             "note": "largest_rectangle returns one int64 (its time includes the read back)"}
+
+
+def run_wide(dev, peak_gbs: float) -> dict:
+    """8-byte keys at N = 2^25 (int64: uniform over the full range, descending,
+    ascending; float64 normal): device time with L2 flushed; useful bytes
+    12 per key (8 in, 4 out)."""
+    import torch
+
+    from apsep_gb300 import Plan
+
+    n = 1 << 25
+    g = torch.Generator(device=dev)
+    g.manual_seed(41)
+    inputs = {
+        "int64_uniform": torch.randint(-(1 << 62), 1 << 62, (n,), generator=g, device=dev, dtype=torch.int64),
+        "int64_descending": torch.arange(n, 0, -1, device=dev, dtype=torch.int64) * (1 << 20),
+        "int64_ascending": torch.arange(n, device=dev, dtype=torch.int64) * (1 << 20),
+        "float64_normal": torch.randn(n, generator=g, device=dev, dtype=torch.float64),
+    }
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    out = torch.empty(n, dtype=torch.int32, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res = {}
+    plans = {torch.int64: Plan(n, torch.int64, device=dev), torch.float64: Plan(n, torch.float64, device=dev)}
+    for name, x in inputs.items():
+        plan = plans[x.dtype]
+        for _ in range(3):
+            plan.run(x, out=out)
+        ts = []
+        for _ in range(9):
+            flush_l2(flush)
+            e0.record()
+            plan.run(x, out=out)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
+        plan.check()
+        ms = statistics.median(ts)
+        gbs = 12.0 * n / ms / 1e6
+        res[name] = {"us": round(ms * 1e3, 1), "gbs": round(gbs, 1), "frac": round(gbs / peak_gbs, 4)}
+    for p in plans.values():
+        p.close()
+    return {"workload": "wide_keys_2p25", "n": n, "bytes_per_key": 12, "runs": res}
 
 
 def run_served(dev) -> dict:
@@ -619,6 +664,8 @@ def run_ours(args) -> None:
         line["served"] = run_served(dev)
         torch.cuda.empty_cache()
         line["consumers"] = run_consumers(dev, peaks["hbm_gbs"])
+        torch.cuda.empty_cache()
+        line["wide"] = run_wide(dev, peaks["hbm_gbs"])
         torch.cuda.empty_cache()
         line["sweep"] = run_sweep(dev, peaks["hbm_gbs"])
     print(json.dumps(line), flush=True)

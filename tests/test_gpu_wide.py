@@ -71,6 +71,17 @@ def test_wide_keys_vs_oracle(plans, dtype, name):
                             (name, n, le, bad, got[bad], want[bad]))
 
 
+def test_float64_signs_and_zeros(plans):
+    """float64 keys compare through an order map of their bits: negative
+    values, both zeros (equal under < and <=), subnormals, huge magnitudes."""
+    rng = np.random.default_rng(99)
+    vals = np.array([-0.0, 0.0, -1.0, 1.0, -5e-324, 5e-324, -1e308, 1e308, 2.5, -2.5], dtype=np.float64)
+    for n in (1000, 100003):
+        a = rng.choice(vals, n)
+        for le in (False, True):
+            assert np.array_equal(run(plans[np.float64], a, le), oracle.apse(a, le)), (n, le)
+
+
 def test_wide_keys_off_a_16_byte_boundary(plans):
     """8-byte aligned but not 16: plain loads and stores throughout."""
     rng = np.random.default_rng(12)
