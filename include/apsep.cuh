@@ -19,8 +19,8 @@
 // APSEP_SHIM_THROW before including to get a std::runtime_error instead.
 // The BLOCK_SIZE / IPT template arguments are accepted for source
 // compatibility; the engine's tile shape comes from its own configuration.
-// Keys: int and float (the reference's ApsepInfinity also lists unsigned,
-// long long, double; those are not supported by the engine and fail to
+// Keys: int, float, long long and double (the reference's ApsepInfinity
+// also lists unsigned, which the engine does not support: it fails to
 // compile here).
 #pragma once
 
@@ -59,6 +59,8 @@ static inline void fail(apsep_status s, const char* what, const char* file, int 
 template <typename T> struct Dtype;
 template <> struct Dtype<int> { static constexpr apsep_dtype value = APSEP_INT32; };
 template <> struct Dtype<float> { static constexpr apsep_dtype value = APSEP_FLOAT32; };
+template <> struct Dtype<long long> { static constexpr apsep_dtype value = APSEP_INT64; };
+template <> struct Dtype<double> { static constexpr apsep_dtype value = APSEP_FLOAT64; };
 
 }  // namespace apsep_shim
 

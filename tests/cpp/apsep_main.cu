@@ -1,7 +1,7 @@
 // apsep_main.cu -- correctness + benchmark harness in the reference's style,
 // written against the drop-in shim (include/apsep.cuh) exactly as code using
 // CoderDue/APSEP's src/apsep.cuh would be.  TEST INFRASTRUCTURE: it links the
-// CPU oracle (oracle/apsep_oracle.c) as its checker.
+// CPU oracle (oracle/apsep_oracle.c) to verify every answer.
 //
 // Same checks as the reference harnesses:
 //   * structured small cases            (src/main.cu:181-222)
@@ -22,6 +22,43 @@
 
 extern "C" int oracle_apse_i32(const int32_t* a, int64_t n, int le, int32_t* out);
 extern "C" int oracle_gen_spt_le_case(int which, int64_t full_n, int64_t n, int32_t* out);
+extern "C" int oracle_apse_i64(const int64_t* a, int64_t n, int le, int32_t* out);
+extern "C" int oracle_apse_f64(const double* a, int64_t n, int le, int32_t* out);
+
+// 8-byte keys through the same names: launchSPT<long long> / <double>.
+static bool wideKeys() {
+    std::mt19937_64 rng(64);
+    bool ok = true;
+    for (int n : {1, 511, 100003}) {
+        std::vector<long long> a(n);
+        std::vector<double> b(n);
+        for (int i = 0; i < n; i++) {
+            a[i] = (long long)rng();
+            b[i] = (double)(long long)(rng() % 1000) * 1e-300;
+        }
+        std::vector<int> ra(n), rb(n), ga(n), gb(n);
+        oracle_apse_i64((const int64_t*)a.data(), n, 0, ra.data());
+        oracle_apse_f64(b.data(), n, 0, rb.data());
+        long long* da;
+        double* db;
+        int* dout;
+        gpuAssert(cudaMalloc(&da, n * sizeof(long long)));
+        gpuAssert(cudaMalloc(&db, n * sizeof(double)));
+        gpuAssert(cudaMalloc(&dout, n * sizeof(int)));
+        gpuAssert(cudaMemcpy(da, a.data(), n * sizeof(long long), cudaMemcpyHostToDevice));
+        gpuAssert(cudaMemcpy(db, b.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        launchSPT<long long>(da, dout, n);
+        gpuAssert(cudaMemcpy(ga.data(), dout, n * sizeof(int), cudaMemcpyDeviceToHost));
+        launchSPT<double>(db, dout, n);
+        gpuAssert(cudaMemcpy(gb.data(), dout, n * sizeof(int), cudaMemcpyDeviceToHost));
+        gpuAssert(cudaFree(da));
+        gpuAssert(cudaFree(db));
+        gpuAssert(cudaFree(dout));
+        ok = ok && ga == ra && gb == rb;
+    }
+    printf("  8-byte keys (long long, double): %s\n", ok ? "PASSED" : "FAILED");
+    return ok;
+}
 
 static std::vector<int> cpuRef(const std::vector<int>& a, bool le = false) {
     std::vector<int> r(a.size());
@@ -200,7 +237,8 @@ int main(int argc, char** argv) {
     ok_s = ok_s && stress(spt, "SPT", t2, 131072, 101);
     printf("  stress WSTL: %s  SPT: %s\n", ok_w ? "PASSED" : "FAILED", ok_s ? "PASSED" : "FAILED");
     bool ok_le = sptLeCases();
-    bool ok = ok_w && ok_s && ok_le;
+    bool ok_wide = wideKeys();
+    bool ok = ok_w && ok_s && ok_le && ok_wide;
     printf("%s\n", ok ? "ALL PASSED" : "CORRECTNESS FAILED");
     if (!ok) return 1;
     if (!quick) benchmark();
