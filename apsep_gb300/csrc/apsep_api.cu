@@ -218,8 +218,7 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
         return APSEP_EINVAL;
     DeviceGuard g(p->device);
     if (!g.ok) return APSEP_ECUDA;
-    if (wide(p->dtype)) {  // 8-byte keys: single arrays, TMA when both arrays are 16-byte aligned
-        if (offsets) return APSEP_ENOTSUP;
+    if (wide(p->dtype)) {  // 8-byte keys: TMA when both arrays are 16-byte aligned
         const int B = kWideTileKeys, key_rows_per_tile = B * 8 / 128;
         int rows = (int)(n / 16);  // 128-byte rows of keys
         CUtensorMap mi, mo;
@@ -242,8 +241,8 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
         a.tma_rows = rows;
         a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
         a.skip_publish_range = p->dbg_skip_range;
-        a.offsets = nullptr;
-        a.nseg = 0;
+        a.offsets = offsets;
+        a.nseg = offsets ? nseg : 0;
         a.s = p->rs;
         p->dbg_skip_range = -1;
         p->dbg_spin_limit = 0;

@@ -140,7 +140,7 @@ cudaError_t range_prepare(int cfg);  // smem attributes + occupancy, current dev
 cudaError_t launch_range_segmented(int dtype, int incl, int cfg, RangeArgs& a, const CUtensorMap& map_in,
                                    const CUtensorMap& map_out, cudaStream_t stream);
 // 8-byte keys (dtype 2: int64, 3: float64): one configuration (8 keys per
-// lane, 8 warps per CTA), single arrays.
+// lane, 8 warps per CTA), single arrays and segmented batches (RangeArgs::offsets).
 constexpr int kWideTileKeys = 256;
 cudaError_t prepare_wide();
 cudaError_t launch_range_wide(int dtype, int incl, RangeArgs& a, const CUtensorMap& map_in,

@@ -8,7 +8,7 @@
 // float64 keys run as int64 through an order-preserving map of their bits
 // (applied as keys enter shared memory or registers): the FP64 compare rate
 // of this part would make every comparison the bottleneck.
-// Single arrays only: one configuration, no segmented form, no view head
+// Single arrays and segmented batches; one configuration; no view head
 // (arrays off a 16-byte boundary take plain loads and stores).
 #include "apsep_range_kernel.cuh"
 
@@ -28,11 +28,15 @@ cudaError_t prepare_wide() {
     if (dev < 0 || dev >= kMaxDevW) return cudaErrorInvalidValue;
     if (g_wide_warps[dev]) return cudaSuccess;
     int per_sm = 0;
-    cudaError_t rr[4] = {prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true>(&per_sm),
+    cudaError_t rr[8] = {prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true>(&per_sm),
                          prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true>(&per_sm),
                          prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true, true>(&per_sm),
-                         prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true, true>(&per_sm)};
-    for (int q = 0; q < 4; q++)
+                         prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true, true>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, false, true, false>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, true, true, false>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, false, true, false, true>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, true, true, false, true>(&per_sm)};
+    for (int q = 0; q < 8; q++)
         if (rr[q] != cudaSuccess) return rr[q];
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -51,9 +55,16 @@ cudaError_t launch_range_wide(int dtype, int incl, RangeArgs& a, const CUtensorM
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     const int max_warps = g_wide_warps[dev];
-    a.offsets = nullptr;
-    a.nseg = 0;
     a.head = 0;
+    if (a.offsets) {  // a segmented batch
+        if (a.nseg < 1) return cudaErrorInvalidValue;
+        if (dtype == 2)
+            return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, true, false>(a, mi, mo, st, max_warps)
+                        : launch_t<int64_t, kWideIpt, kWideWpc, false, true, false>(a, mi, mo, st, max_warps);
+        return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, true, false, true>(a, mi, mo, st, max_warps)
+                    : launch_t<int64_t, kWideIpt, kWideWpc, false, true, false, true>(a, mi, mo, st, max_warps);
+    }
+    a.nseg = 0;
     if (dtype == 2)
         return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, false, true>(a, mi, mo, st, max_warps)
                     : launch_t<int64_t, kWideIpt, kWideWpc, false, false, true>(a, mi, mo, st, max_warps);
