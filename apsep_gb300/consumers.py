@@ -24,8 +24,8 @@ def workspace_bytes(n: int) -> int:
 
 
 def _prep(x: torch.Tensor, plan: Plan | None, work: torch.Tensor | None):
-    if not x.is_cuda or x.dtype not in (torch.int32, torch.float32):
-        raise ValueError("x must be a CUDA int32 or float32 tensor (there is no CPU path)")
+    if not x.is_cuda or x.dtype not in (torch.int32, torch.float32, torch.int64, torch.float64):
+        raise ValueError("x must be a CUDA int32, float32, int64 or float64 tensor (there is no CPU path)")
     x = x.contiguous()
     n = x.numel()
     own = plan is None

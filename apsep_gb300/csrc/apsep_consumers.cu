@@ -16,6 +16,8 @@
 // synchronisation, graph-capturable like apsep_run.
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "apsep.h"
 #include "apsep_internal.h"
 
@@ -34,6 +36,33 @@ size_t align16(size_t x) { return (x + 15) / 16 * 16; }
 // float: -x, the two zeros stay equal).
 __device__ __forceinline__ int32_t flip(int32_t x) { return ~x; }
 __device__ __forceinline__ float flip(float x) { return -x; }
+__device__ __forceinline__ int64_t flip(int64_t x) { return ~x; }
+__device__ __forceinline__ double flip(double x) { return -x; }
+
+int key_bytes(int dtype) { return dtype == APSEP_INT64 || dtype == APSEP_FLOAT64 ? 8 : 4; }
+
+// Calls f(T*) with a null pointer of the plan's key type.
+template <typename F>
+void for_key_type(int dtype, F&& f) {
+    switch (dtype) {
+    case APSEP_INT32: f((int32_t*)nullptr); break;
+    case APSEP_FLOAT32: f((float*)nullptr); break;
+    case APSEP_INT64: f((int64_t*)nullptr); break;
+    default: f((double*)nullptr); break;
+    }
+}
+
+// Workspace: the keys (n of the plan's type), then two answer arrays.
+struct Work {
+    void* keys;
+    int32_t* a;
+    int32_t* b;
+};
+Work carve(void* d_work, int64_t n, int dtype) {
+    char* w = (char*)d_work;
+    const size_t kb = align16((size_t)n * key_bytes(dtype)), ab = align16((size_t)n * 4);
+    return {w, (int32_t*)(w + kb), (int32_t*)(w + kb + ab)};
+}
 
 template <typename T>
 __global__ void flip_keys(const T* __restrict__ in, T* __restrict__ out, int64_t n) {
@@ -119,11 +148,11 @@ apsep_status check_args(apsep_plan* plan, const void* d_in, const void* d_out, s
     const apsep_status s = apsep_plan_get_info(plan, &info);
     if (s != APSEP_OK) return s;
     *dtype = info.dtype;
-    if (info.dtype != APSEP_INT32 && info.dtype != APSEP_FLOAT32) return APSEP_ENOTSUP;  // 4-byte keys
     if (n == 0) return APSEP_OK;
     if (n > info.capacity || !d_in || !d_out || !d_work) return APSEP_EINVAL;
-    if ((uintptr_t)d_work % 16 != 0 || (uintptr_t)d_in % 4 != 0) return APSEP_EINVAL;
-    const size_t wb = (size_t)apsep_consumer_workspace_bytes(n), kb = (size_t)n * 4;
+    const size_t kb = (size_t)n * key_bytes(info.dtype);
+    if ((uintptr_t)d_work % 16 != 0 || (uintptr_t)d_in % key_bytes(info.dtype) != 0) return APSEP_EINVAL;
+    const size_t wb = (size_t)apsep_consumer_workspace_bytes(n);
     if (overlaps(d_work, wb, d_in, kb) || overlaps(d_work, wb, d_out, out_bytes)) return APSEP_EINVAL;
     return APSEP_OK;
 }
@@ -136,7 +165,7 @@ extern "C" {
 
 int64_t apsep_consumer_workspace_bytes(int64_t n) {
     if (n < 0) return 0;
-    return (int64_t)(3 * align16((size_t)n * 4));
+    return (int64_t)(align16((size_t)n * 8) + 2 * align16((size_t)n * 4));  // any key type
 }
 
 apsep_status apsep_run_prev_greater(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
@@ -145,10 +174,10 @@ apsep_status apsep_run_prev_greater(apsep_plan* plan, const void* d_in, int32_t*
     apsep_status s = check_args(plan, d_in, d_out, (size_t)n * 4, n, d_work, &dtype);
     if (s != APSEP_OK || n == 0) return s;
     const cudaStream_t st = (cudaStream_t)stream;
-    if (dtype == APSEP_FLOAT32)
-        flip_keys<float><<<grid_for(n), kThreads, 0, st>>>((const float*)d_in, (float*)d_work, n);
-    else
-        flip_keys<int32_t><<<grid_for(n), kThreads, 0, st>>>((const int32_t*)d_in, (int32_t*)d_work, n);
+    for_key_type(dtype, [&](auto tag) {
+        using T = std::remove_pointer_t<decltype(tag)>;
+        flip_keys<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, (T*)d_work, n);
+    });
     if ((s = launched()) != APSEP_OK) return s;
     return apsep_run_cmp(plan, d_work, d_out, n, cmp, stream);
 }
@@ -159,15 +188,14 @@ apsep_status apsep_run_next_smaller(apsep_plan* plan, const void* d_in, int32_t*
     apsep_status s = check_args(plan, d_in, d_out, (size_t)n * 4, n, d_work, &dtype);
     if (s != APSEP_OK || n == 0) return s;
     const cudaStream_t st = (cudaStream_t)stream;
-    char* w = (char*)d_work;
-    int32_t* wa = (int32_t*)(w + align16((size_t)n * 4));
-    if (dtype == APSEP_FLOAT32)
-        reverse_keys<float><<<grid_for(n), kThreads, 0, st>>>((const float*)d_in, (float*)w, n);
-    else
-        reverse_keys<int32_t><<<grid_for(n), kThreads, 0, st>>>((const int32_t*)d_in, (int32_t*)w, n);
+    const Work w = carve(d_work, n, dtype);
+    for_key_type(dtype, [&](auto tag) {
+        using T = std::remove_pointer_t<decltype(tag)>;
+        reverse_keys<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, (T*)w.keys, n);
+    });
     if ((s = launched()) != APSEP_OK) return s;
-    if ((s = apsep_run_cmp(plan, w, wa, n, cmp, stream)) != APSEP_OK) return s;
-    mirror_answers<<<grid_for(n), kThreads, 0, st>>>(wa, d_out, n);
+    if ((s = apsep_run_cmp(plan, w.keys, w.a, n, cmp, stream)) != APSEP_OK) return s;
+    mirror_answers<<<grid_for(n), kThreads, 0, st>>>(w.a, d_out, n);
     return launched();
 }
 
@@ -189,14 +217,12 @@ apsep_status apsep_largest_rectangle(apsep_plan* plan, const int32_t* d_heights,
     const cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(d_area, 0, 8, st) != cudaSuccess) return APSEP_ECUDA;
     if (n == 0) return APSEP_OK;
-    char* w = (char*)d_work;
-    int32_t* wa = (int32_t*)(w + align16((size_t)n * 4));
-    int32_t* wl = (int32_t*)(w + 2 * align16((size_t)n * 4));
-    if ((s = apsep_run_cmp(plan, d_heights, wl, n, APSEP_LT, stream)) != APSEP_OK) return s;
-    reverse_keys<int32_t><<<grid_for(n), kThreads, 0, st>>>(d_heights, (int32_t*)w, n);
+    const Work w = carve(d_work, n, dtype);
+    if ((s = apsep_run_cmp(plan, d_heights, w.b, n, APSEP_LT, stream)) != APSEP_OK) return s;
+    reverse_keys<int32_t><<<grid_for(n), kThreads, 0, st>>>(d_heights, (int32_t*)w.keys, n);
     if ((s = launched()) != APSEP_OK) return s;
-    if ((s = apsep_run_cmp(plan, w, wa, n, APSEP_LT, stream)) != APSEP_OK) return s;
-    rect_area<<<grid_for(n), kThreads, 0, st>>>(d_heights, wl, wa, n, (unsigned long long*)d_area);
+    if ((s = apsep_run_cmp(plan, w.keys, w.a, n, APSEP_LT, stream)) != APSEP_OK) return s;
+    rect_area<<<grid_for(n), kThreads, 0, st>>>(d_heights, w.b, w.a, n, (unsigned long long*)d_area);
     return launched();
 }
 
@@ -206,20 +232,18 @@ apsep_status apsep_cartesian_parents(apsep_plan* plan, const void* d_in, int32_t
     apsep_status s = check_args(plan, d_in, d_out, (size_t)n * 4, n, d_work, &dtype);
     if (s != APSEP_OK || n == 0) return s;
     const cudaStream_t st = (cudaStream_t)stream;
-    char* w = (char*)d_work;
-    int32_t* wa = (int32_t*)(w + align16((size_t)n * 4));
-    int32_t* wl = (int32_t*)(w + 2 * align16((size_t)n * 4));
-    if ((s = apsep_run_cmp(plan, d_in, wl, n, APSEP_LE, stream)) != APSEP_OK) return s;
-    if (dtype == APSEP_FLOAT32)
-        reverse_keys<float><<<grid_for(n), kThreads, 0, st>>>((const float*)d_in, (float*)w, n);
-    else
-        reverse_keys<int32_t><<<grid_for(n), kThreads, 0, st>>>((const int32_t*)d_in, (int32_t*)w, n);
+    const Work w = carve(d_work, n, dtype);
+    if ((s = apsep_run_cmp(plan, d_in, w.b, n, APSEP_LE, stream)) != APSEP_OK) return s;
+    for_key_type(dtype, [&](auto tag) {
+        using T = std::remove_pointer_t<decltype(tag)>;
+        reverse_keys<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, (T*)w.keys, n);
+    });
     if ((s = launched()) != APSEP_OK) return s;
-    if ((s = apsep_run_cmp(plan, w, wa, n, APSEP_LT, stream)) != APSEP_OK) return s;
-    if (dtype == APSEP_FLOAT32)
-        cartesian_parent<float><<<grid_for(n), kThreads, 0, st>>>((const float*)d_in, wl, wa, d_out, n);
-    else
-        cartesian_parent<int32_t><<<grid_for(n), kThreads, 0, st>>>((const int32_t*)d_in, wl, wa, d_out, n);
+    if ((s = apsep_run_cmp(plan, w.keys, w.a, n, APSEP_LT, stream)) != APSEP_OK) return s;
+    for_key_type(dtype, [&](auto tag) {
+        using T = std::remove_pointer_t<decltype(tag)>;
+        cartesian_parent<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, w.b, w.a, d_out, n);
+    });
     return launched();
 }
 

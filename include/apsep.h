@@ -51,9 +51,9 @@ typedef enum apsep_status {
 
 /* Key types.  8-byte keys (the reference's ApsepInfinity<long long/double>,
  * src/apsep.cuh:62-70) keep int32 positions (n <= APSEP_MAX_KEYS) and run
- * single arrays and segmented batches; apsep_run_noalloc and the consumers
- * refuse them (APSEP_EINVAL / APSEP_ENOTSUP), and their plans have one
- * configuration (1). */
+ * single arrays, segmented batches and the consumers (the histogram takes
+ * int32 heights); apsep_run_noalloc refuses them (APSEP_EINVAL), and their
+ * plans have one configuration (1). */
 typedef enum apsep_dtype { APSEP_INT32 = 0, APSEP_FLOAT32 = 1, APSEP_INT64 = 2, APSEP_FLOAT64 = 3 } apsep_dtype;
 
 typedef enum apsep_cmp {

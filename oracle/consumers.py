@@ -84,7 +84,7 @@ def cartesian_parents_stack(a) -> np.ndarray:
 
 # ---- compositions with the C oracle (any size) -----------------------------
 def _flip(a: np.ndarray) -> np.ndarray:
-    return ~a if a.dtype == np.int32 else -a
+    return ~a if np.issubdtype(a.dtype, np.integer) else -a
 
 
 def prev_greater(a: np.ndarray, le: bool = False) -> np.ndarray:

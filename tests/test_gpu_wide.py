@@ -135,8 +135,24 @@ def test_wide_unsupported_forms(plans):
     assert lib.apsep_run_noalloc(vp(x.data_ptr()), vp(o.data_ptr()), 100, _lib.INT64, _lib.LT,
                                  None) == _lib.APSEP_EINVAL
     from apsep_gb300 import consumers
-    with pytest.raises(ValueError):  # the Python mirror refuses before the call
-        consumers.stock_span(x, plan=plan)
     w = torch.empty(consumers.workspace_bytes(1000), dtype=torch.uint8, device="cuda")
-    assert lib.apsep_stock_span(plan._h, vp(x.data_ptr()), vp(o.data_ptr()), 1000, vp(w.data_ptr()),
-                                None) == _lib.APSEP_ENOTSUP
+    area = torch.zeros(1, dtype=torch.int64, device="cuda")
+    assert lib.apsep_largest_rectangle(plan._h, vp(x.data_ptr()), 1000, vp(area.data_ptr()), vp(w.data_ptr()),
+                                       None) == _lib.APSEP_ENOTSUP  # the histogram takes int32 heights
+
+
+@pytest.mark.parametrize("dtype", [np.int64, np.float64])
+def test_wide_consumers(plans, dtype):
+    from oracle import consumers as oc
+    from apsep_gb300 import consumers
+    rng = np.random.default_rng(31)
+    for name in ("uniform", "lowbits", "dup16"):
+        a = keys(name, 100003, rng, dtype)
+        x = torch.from_numpy(a).cuda()
+        plan = plans[dtype]
+        for le in (False, True):
+            assert np.array_equal(consumers.prev_greater(x, le, plan=plan).cpu().numpy(), oc.prev_greater(a, le))
+            assert np.array_equal(consumers.next_smaller(x, le, plan=plan).cpu().numpy(), oc.next_smaller(a, le))
+        assert np.array_equal(consumers.stock_span(x, plan=plan).cpu().numpy(), oc.stock_span(a))
+        assert np.array_equal(consumers.cartesian_parents(x, plan=plan).cpu().numpy(), oc.cartesian_parents(a))
+        plan.check()
