@@ -46,19 +46,14 @@ template <> struct KeyTraits<float> {
     }
 };
 
-// 8-byte keys (int64 / float64, with int32 positions): bits are the raw
-// 64-bit pattern; their status words keep the key apart from the tag.
+// 8-byte keys (int64, and float64 through f64_order below), with int32
+// positions: bits are the raw 64-bit pattern; their status words keep the
+// key apart from the tag.
 template <> struct KeyTraits<int64_t> {
     __device__ __forceinline__ static int64_t pad() { return LLONG_MAX; }
     __device__ __forceinline__ static int64_t vmin(int64_t a, int64_t b) { return a < b ? a : b; }
     __device__ __forceinline__ static uint64_t bits(int64_t a) { return (uint64_t)a; }
     __device__ __forceinline__ static int64_t from_bits(uint64_t b) { return (int64_t)b; }
-};
-template <> struct KeyTraits<double> {
-    __device__ __forceinline__ static double pad() { return __longlong_as_double(0x7ff0000000000000LL); }  // +inf
-    __device__ __forceinline__ static double vmin(double a, double b) { return fmin(a, b); }
-    __device__ __forceinline__ static uint64_t bits(double a) { return (uint64_t)__double_as_longlong(a); }
-    __device__ __forceinline__ static double from_bits(uint64_t b) { return __longlong_as_double((long long)b); }
 };
 
 // float64 keys compare as int64 (the FP64 pipe is slow on this part): the
