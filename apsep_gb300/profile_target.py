@@ -1,9 +1,10 @@
 """Minimal profiling target (the role of the reference's src/profile_bottleneck.cu).
 
     python -m apsep_gb300.profile_target [--dist uniform|descending|ascending|dup16]
-                                         [--n 33554432] [--reps 3] [--config 0] [--dtype int32|float32]
+                                         [--n 33554432] [--reps 3] [--config 0]
+                                         [--dtype int32|float32|int64|float64]
 
-Allocates one input and one output (2 * 4 * n bytes), runs `reps` APSE
+Allocates one input and one output ((4 or 8) * n + 4 * n bytes), runs `reps` APSE
 launches with a synchronisation after each, prints the last launch's time.
 Small enough on the device for ncu captures; n = 2^25 keeps the 128 MiB
 input above the 126 MiB L2.
@@ -24,7 +25,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=1 << 25)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--config", type=int, default=0)
-    ap.add_argument("--dtype", default="int32", choices=("int32", "float32"))
+    ap.add_argument("--dtype", default="int32", choices=("int32", "float32", "int64", "float64"))
     a = ap.parse_args()
     rng = np.random.default_rng(7)
     n = a.n
@@ -36,11 +37,12 @@ def main() -> None:
         h = np.arange(n, dtype=np.int64)
     else:
         h = rng.integers(0, 16, n)
-    dt = torch.int32 if a.dtype == "int32" else torch.float32
-    x = torch.from_numpy(h.astype(np.int32 if a.dtype == "int32" else np.float32)).cuda()
+    dt = getattr(torch, a.dtype)
+    x = torch.from_numpy(h.astype(getattr(np, a.dtype))).cuda()
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     plan = Plan(n, dt)
-    plan.set_config(a.config)
+    if dt in (torch.int32, torch.float32):
+        plan.set_config(a.config)  # (8-byte keys have one configuration)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     times = []
     for _ in range(a.reps):
@@ -52,8 +54,9 @@ def main() -> None:
         times.append(e0.elapsed_time(e1) * 1e3)
     t = sorted(times[1:] if len(times) > 1 else times)
     med = t[len(t) // 2]
-    print("done dist=%s n=%d config=%d median=%.1f us min=%.1f max=%.1f (%.1f GB/s useful at the median)"
-          % (a.dist, n, a.config, med, t[0], t[-1], 8.0 * n / (med * 1e-6) / 1e9))
+    kb = x.element_size()
+    print("done dist=%s dtype=%s n=%d median=%.1f us min=%.1f max=%.1f (%.1f GB/s useful at the median)"
+          % (a.dist, a.dtype, n, med, t[0], t[-1], (kb + 4.0) * n / (med * 1e-6) / 1e9))
     plan.close()
 
 
