@@ -11,6 +11,7 @@ from .api import (  # noqa: F401
     alloc_spt_scratch,
     alloc_wstl_scratch,
     apse,
+    apse64,
     apse_segmented,
     free_spt_scratch,
     free_wstl_scratch,

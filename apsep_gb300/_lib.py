@@ -37,10 +37,13 @@ SIGNATURES = {
     "apsep_stock_span": ([_vp, _vp, _vp, _i64, _vp, _vp], ctypes.c_int),
     "apsep_largest_rectangle": ([_vp, _vp, _i64, _vp, _vp, _vp], ctypes.c_int),
     "apsep_cartesian_parents": ([_vp, _vp, _vp, _i64, _vp, _vp], ctypes.c_int),
+    "apsep_run64_workspace_bytes": ([_vp, _i64], _i64),
+    "apsep_run64": ([_vp, _vp, _vp, _i64, ctypes.c_int, _vp, _vp], ctypes.c_int),
 }
 
 NOALLOC_MAX_KEYS = 4194304  # APSEP_NOALLOC_MAX_KEYS in include/apsep.h
 MAX_KEYS = 2147479552  # APSEP_MAX_KEYS in include/apsep.h (2^31 - 4096)
+MAX_KEYS64 = 1 << 40  # APSEP_MAX_KEYS64 in include/apsep.h
 
 APSEP_OK, APSEP_EINVAL, APSEP_ENOMEM, APSEP_ECUDA, APSEP_ETIMEOUT, APSEP_EINTERNAL, APSEP_ENOTSUP = range(7)
 INT32, FLOAT32, INT64, FLOAT64 = 0, 1, 2, 3

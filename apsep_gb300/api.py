@@ -127,6 +127,37 @@ class Plan:
         _lib.check(st, "apsep_run_segmented")
         return out
 
+    def workspace64_bytes(self, n: int) -> int:
+        """Device workspace of run64 over n keys (-1: n out of range)."""
+        return int(self._lib.apsep_run64_workspace_bytes(self._h, int(n)))
+
+    def run64(self, x: torch.Tensor, out: torch.Tensor | None = None, inclusive: bool | None = None,
+              work: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """Enqueue out = APSE(x) with int64 positions, for x of any length up
+        to MAX_KEYS64: consecutive pieces of this plan's capacity, keys that
+        their own piece does not answer answered from a hierarchy of minima
+        over the keys before it (apsep_run64)."""
+        if not x.is_cuda or x.dtype != self.dtype or not x.is_contiguous():
+            raise ValueError("x must be a contiguous CUDA %s tensor" % self.dtype)
+        n = x.numel()
+        if out is None:
+            out = torch.empty(n, dtype=torch.int64, device=x.device)
+        if out.dtype != torch.int64 or not out.is_cuda or not out.is_contiguous() or out.numel() < n:
+            raise ValueError("out must be a contiguous CUDA int64 tensor of x.numel() entries")
+        need = self.workspace64_bytes(n)
+        if need < 0:
+            raise ValueError("n = %d is out of range for run64 on this plan" % n)
+        if work is None:
+            work = torch.empty(max(need, 16), dtype=torch.uint8, device=x.device)
+        elif not work.is_cuda or work.numel() * work.element_size() < need:
+            raise ValueError("work must be a CUDA buffer of at least %d bytes" % need)
+        incl = self.inclusive if inclusive is None else bool(inclusive)
+        st = self._lib.apsep_run64(self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), n,
+                                   _lib.LE if incl else _lib.LT, ctypes.c_void_p(work.data_ptr()),
+                                   ctypes.c_void_p(_stream_handle(x.device, stream)))
+        _lib.check(st, "apsep_run64")
+        return out
+
     def check(self, stream=None) -> None:
         """Synchronise and raise on device-side errors of earlier runs."""
         _lib.check(self._lib.apsep_plan_check(self._h, ctypes.c_void_p(_stream_handle(self.device, stream))),
@@ -188,6 +219,24 @@ def apse_segmented(x: torch.Tensor, offsets: torch.Tensor, inclusive: bool = Fal
             plan = Plan(max(x.numel(), 1 << 16), x.dtype, inclusive=inclusive, device=x.device)
         _cache[key] = plan
     return plan.run_segmented(x, offsets, out=out)
+
+
+def apse64(x: torch.Tensor, inclusive: bool = False, out: torch.Tensor | None = None) -> torch.Tensor:
+    """One call with int64 positions, for x of any length up to MAX_KEYS64
+    (pieces of at most MAX_KEYS keys; see Plan.run64)."""
+    if not x.is_cuda:
+        raise ValueError("apse64 runs on CUDA tensors only (there is no CPU path)")
+    x = x.contiguous()
+    key = (x.device, x.dtype, "64")
+    cap = min(max(x.numel(), 1 << 16), _lib.MAX_KEYS)
+    plan = _cache.get(key)
+    if plan is None or plan.capacity < cap:
+        if plan is not None:
+            plan.close()
+        with torch.cuda.device(x.device):
+            plan = Plan(cap, x.dtype, device=x.device)
+        _cache[key] = plan
+    return plan.run64(x, out=out, inclusive=inclusive)
 
 
 # ---------------------------------------------------------------------------

@@ -95,6 +95,8 @@ bool ranges_overlap(const void* a, size_t an, const void* b, size_t bn) {
 
 }  // namespace
 
+uint32_t* plan_error_word(apsep_plan* p) { return &p->rs.ctr->err; }
+
 extern "C" {
 
 int apsep_version(void) { return 10000; }

@@ -155,3 +155,8 @@ cudaError_t prepare_segmented(int cfg, int* ctas_per_sm);
 cudaError_t range_max_warps(int cfg, int* warps);  // persistent warps of one launch, current device
 
 }  // namespace apsep
+
+// The plan's sticky device-side error word (ERR_* bits, read by
+// apsep_plan_check), for passes that run around the engine.
+struct apsep_plan;
+uint32_t* plan_error_word(struct apsep_plan* plan);

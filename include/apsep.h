@@ -192,6 +192,25 @@ apsep_status apsep_largest_rectangle(apsep_plan* plan, const int32_t* d_heights,
 apsep_status apsep_cartesian_parents(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, void* d_work,
                                      void* stream);
 
+/* ---- 64-bit positions: arrays of any length -------------------------------
+ * d_out[i] (int64) = the largest j < i with a[j] < a[i] (APSEP_LT) or
+ * a[j] <= a[i] (APSEP_LE), else -1, for n up to APSEP_MAX_KEYS64 keys of the
+ * plan's type: the reference's entry points take `int n`
+ * (src/apsep.cuh:3052-3076) while its key types anticipate longer arrays
+ * (src/apsep.cuh:62-70).  The array runs as consecutive pieces of the plan's
+ * capacity (rounded down to whole 32-key groups; the whole array when
+ * n <= capacity), one engine run each; keys that no key of their own piece
+ * answers are answered from a hierarchy of minima over the keys before the
+ * piece.  d_work: a 16-byte aligned device workspace of
+ * apsep_run64_workspace_bytes(plan, n) bytes (-1: n out of range, or a plan
+ * with capacity < 32 for n > capacity), not overlapping the keys or d_out
+ * (8-byte aligned).  Asynchronous on `stream`; device-side errors surface
+ * through apsep_plan_check. */
+#define APSEP_MAX_KEYS64 1099511627776LL /* 2^40 */
+int64_t apsep_run64_workspace_bytes(const apsep_plan* plan, int64_t n);
+apsep_status apsep_run64(apsep_plan* plan, const void* d_in, int64_t* d_out, int64_t n, apsep_cmp cmp,
+                         void* d_work, void* stream);
+
 /* Fault injection for failure-detection tests: in the next run, range `range`
  * (the contiguous block of tiles one persistent CTA sweeps) never publishes
  * its look-back status, and every device wait gives up after `spin_limit`
