@@ -25,6 +25,7 @@ struct apsep_plan {
     RangeScratch rs{};
     int dbg_skip_range = -1;
     uint32_t dbg_spin_limit = 0;
+    int last_head = 0;  // view head of the last single-array run (its chunk minima sit shifted by it)
 };
 
 namespace {
@@ -96,6 +97,7 @@ bool ranges_overlap(const void* a, size_t an, const void* b, size_t bn) {
 }  // namespace
 
 uint32_t* plan_error_word(apsep_plan* p) { return &p->rs.ctr->err; }
+const void* plan_chunk_minima(apsep_plan* p) { return p->last_head == 0 ? p->rs.chunk_min : nullptr; }
 
 extern "C" {
 
@@ -248,6 +250,7 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
         a.s = p->rs;
         p->dbg_skip_range = -1;
         p->dbg_spin_limit = 0;
+        p->last_head = 0;
         const cudaError_t e = launch_range_wide(p->dtype, cmp == APSEP_LE ? 1 : 0, a, mi, mo, (cudaStream_t)stream);
         return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
     }
@@ -289,6 +292,7 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
     a.s = p->rs;
     p->dbg_skip_range = -1;  // one-shot
     p->dbg_spin_limit = 0;
+    p->last_head = head;
     const int incl = cmp == APSEP_LE ? 1 : 0;
     cudaError_t e = offsets ? launch_range_segmented(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
                     : head  ? launch_range_view(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)

@@ -160,3 +160,7 @@ cudaError_t range_max_warps(int cfg, int* warps);  // persistent warps of one la
 // apsep_plan_check), for passes that run around the engine.
 struct apsep_plan;
 uint32_t* plan_error_word(struct apsep_plan* plan);
+// The minimum of every 32 keys of the plan's last single-array run (written
+// by its phase 1, in key order), or null when that run sat behind a view
+// head (its chunks then start `head` keys before the array).
+const void* plan_chunk_minima(struct apsep_plan* plan);

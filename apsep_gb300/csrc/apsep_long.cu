@@ -42,6 +42,7 @@ namespace {
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int kLevels = 9;  // levels 0..8: 32^8 = 2^40 >= APSEP_MAX_KEYS64
 constexpr int kThreads = 256;
+constexpr int kU = 4;  // 32-key groups per warp and step of the widening pass
 
 size_t align16(size_t x) { return (x + 15) / 16 * 16; }
 int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
@@ -146,50 +147,79 @@ __device__ int64_t answer_before(const K* keys, const Levels<K>& lv, K q, int l,
 
 // Piece [b0, b1): out[i] = b0 + t32[i - b0] when the piece answers key i,
 // else the answer before b0 (or -1).  With build_l1, also the level-1 minima
-// of the piece's 32-key groups.
+// of the piece's 32-key groups: copied from the engine run's own chunk
+// minima (cmin) when it has them in key order, else taken over the keys.
 template <typename K, bool MAPF, bool INCL>
 __global__ void __launch_bounds__(kThreads)
     widen_kernel(const K* __restrict__ keys, const int32_t* __restrict__ t32, int64_t* __restrict__ out, int64_t b0,
                  int64_t b1, Levels<K> lv, const Frontier<K>* __restrict__ fr, bool look_before, bool build_l1,
-                 uint32_t* err) {
+                 const K* __restrict__ cmin, uint32_t* err) {
     __shared__ K su[kLevels];
+    __shared__ K spm;  // the minimum of everything before b0
     __shared__ uint32_t shas;
     if (threadIdx.x < kLevels) su[threadIdx.x] = look_before ? fr->u[threadIdx.x] : KeyTraits<K>::pad();
-    if (threadIdx.x == 0) shas = look_before ? fr->has : 0u;
+    if (threadIdx.x == 0) {
+        const uint32_t h = look_before ? fr->has : 0u;
+        K m = KeyTraits<K>::pad();
+        for (int l = 0; l < kLevels; l++)
+            if ((h >> l) & 1u) m = KeyTraits<K>::vmin(m, fr->u[l]);
+        spm = m;
+        shas = h;
+    }
     __syncthreads();
     const uint32_t has = shas;
+    const K pm = spm;
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t ngroups = (b1 - b0 + 31) >> 5;
-    const bool need_keys = has != 0 || build_l1;
-    for (int64_t g = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); g < ngroups; g += nw) {
-        const int64_t i = b0 + (g << 5) + lane;
-        const bool valid = i < b1;
-        const int32_t t = valid ? __ldcs(t32 + (i - b0)) : 0;
-        const K k = need_keys && valid ? load_key<K, MAPF>(keys + i) : KeyTraits<K>::pad();
-        if (build_l1) {
-            const K m = warp_min(k);
-            if (lane == 0) lv.p[1][(b0 >> 5) + g] = m;
+    const bool all_keys = build_l1 && !cmin;  // every key, for the level-1 minima
+    // kU groups of 32 keys per warp and step, their loads issued together
+    for (int64_t g0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kU; g0 < ngroups; g0 += nw * kU) {
+        int32_t t[kU];
+        K k[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int64_t i = b0 + ((g0 + u) << 5) + lane;
+            t[u] = i < b1 ? __ldcs(t32 + (i - b0)) : 0;
         }
-        int64_t o = t >= 0 ? b0 + t : -1;
-        int lvl = -1;  // the nearest frontier whose minimum qualifies
-        if (valid && t < 0 && has) {
-            for (int l = 0; l < kLevels; l++)
-                if (((has >> l) & 1u) && lt<INCL>(su[l], k)) {
-                    lvl = l;
-                    break;
-                }
+        // a key is read for the level-1 minima, or when the piece does not answer it
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int64_t i = b0 + ((g0 + u) << 5) + lane;
+            k[u] = i < b1 && (all_keys || (has && t[u] < 0)) ? load_key<K, MAPF>(keys + i) : KeyTraits<K>::pad();
         }
-        unsigned qm = __ballot_sync(FULL, lvl >= 0);
-        while (qm) {
-            const int src = __ffs(qm) - 1;
-            qm &= qm - 1;
-            const K q = __shfl_sync(FULL, k, src);
-            const int l = __shfl_sync(FULL, lvl, src);
-            const int64_t ans = answer_before<K, MAPF, INCL>(keys, lv, q, l, b0, err);
-            if (lane == src) o = ans;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int64_t g = g0 + u;
+            if (g >= ngroups) break;
+            const int64_t i = b0 + (g << 5) + lane;
+            const bool valid = i < b1;
+            if (all_keys) {
+                const K m = warp_min(k[u]);
+                if (lane == 0) lv.p[1][(b0 >> 5) + g] = m;
+            } else if (build_l1 && lane == 0) {
+                lv.p[1][(b0 >> 5) + g] = __ldcs(cmin + g);
+            }
+            int64_t o = t[u] >= 0 ? b0 + t[u] : -1;
+            int lvl = -1;  // the nearest frontier whose minimum qualifies
+            if (valid && t[u] < 0 && has && lt<INCL>(pm, k[u])) {
+                for (int l = 0; l < kLevels; l++)
+                    if (((has >> l) & 1u) && lt<INCL>(su[l], k[u])) {
+                        lvl = l;
+                        break;
+                    }
+            }
+            unsigned qm = __ballot_sync(FULL, lvl >= 0);
+            while (qm) {
+                const int src = __ffs(qm) - 1;
+                qm &= qm - 1;
+                const K q = __shfl_sync(FULL, k[u], src);
+                const int l = __shfl_sync(FULL, lvl, src);
+                const int64_t ans = answer_before<K, MAPF, INCL>(keys, lv, q, l, b0, err);
+                if (lane == src) o = ans;
+            }
+            if (valid) __stcs(reinterpret_cast<long long*>(out) + i, (long long)o);
         }
-        if (valid) __stcs(reinterpret_cast<long long*>(out) + i, (long long)o);
     }
 }
 
@@ -231,18 +261,23 @@ apsep_status run_long(apsep_plan* plan, const K* keys, int64_t* out, int64_t n, 
     const Levels<K> lv = make_levels<K>(w, n, pieces);
     Frontier<K>* fr = (Frontier<K>*)w.front;
     uint32_t* err = plan_error_word(plan);
-    const int grid = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(piece, kThreads * 4), 1), 152 * 8);
+    // one wave of resident blocks at most (the pass strides over its groups)
+    auto widen = cmp == APSEP_LE ? widen_kernel<K, MAPF, true> : widen_kernel<K, MAPF, false>;
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, widen, kThreads, 0) != cudaSuccess)
+        return APSEP_ECUDA;
+    const int64_t keys_per_block = (int64_t)kThreads * kU;  // per step
+    const int grid = (int)std::min<int64_t>(std::max<int64_t>(ceil_div(piece, keys_per_block), 1),
+                                            (int64_t)sms * std::max(per_sm, 1));
     for (int64_t b0 = 0; b0 < n; b0 += piece) {
         const int64_t b1 = std::min(n, b0 + piece);
         apsep_status s = apsep_run_cmp(plan, keys + b0, w.t32, b1 - b0, cmp, st);
         if (s != APSEP_OK) return s;
         const bool look = b0 > 0;
         if (look) frontier_kernel<K, MAPF><<<1, 32, 0, st>>>(keys, lv, b0, fr);
-        if (cmp == APSEP_LE)
-            widen_kernel<K, MAPF, true><<<grid, kThreads, 0, st>>>(keys, w.t32, out, b0, b1, lv, fr, look, pieces, err);
-        else
-            widen_kernel<K, MAPF, false><<<grid, kThreads, 0, st>>>(keys, w.t32, out, b0, b1, lv, fr, look, pieces,
-                                                                    err);
+        const K* cmin = (const K*)plan_chunk_minima(plan);  // this piece's, when in key order
+        widen<<<grid, kThreads, 0, st>>>(keys, w.t32, out, b0, b1, lv, fr, look, pieces, cmin, err);
         if (cudaGetLastError() != cudaSuccess) return APSEP_ECUDA;
         if (!pieces || b1 == n) continue;
         // level entries that complete inside this piece (level 1 came with the pass)
@@ -251,7 +286,7 @@ apsep_status run_long(apsep_plan* plan, const K* keys, int64_t* out, int64_t n, 
             span *= 32;
             const int64_t e_lo = b0 / span, e_hi = b1 / span;
             if (e_hi > e_lo) {
-                const int g = (int)std::min<int64_t>(ceil_div(e_hi - e_lo, kThreads / 32), 152 * 8);
+                const int g = (int)std::min<int64_t>(ceil_div(e_hi - e_lo, kThreads / 32), (int64_t)sms * 8);
                 level_kernel<K><<<g, kThreads, 0, st>>>(lv.p[l - 1], lv.size[l - 1], lv.p[l], e_lo, e_hi);
             }
         }

@@ -51,6 +51,9 @@ Extra objects on the same line (one GPU only; --no-extras skips them):
              useful GB/s and the fraction of peak of all their HBM passes.
   wide       8-byte keys (int64 / float64) at N = 2^25: time, useful GB/s
              (12 B/key) and fraction of peak.
+  long64     int64 positions beyond 2^31 keys (Plan.run64): N = 2^32 int32
+             keys in two pieces of 2^31 - 4096, uniform and descending; time,
+             useful GB/s (12 B/key: 4 in, 8 out) and fraction of peak.
   sweep      single-array useful GB/s and roofline fraction for N = 2^14 ..
              2^30 (every second power of two), uniform and descending keys.
 
@@ -370,6 +373,49 @@ def run_wide(dev, peak_gbs: float) -> dict:
     return {"workload": "wide_keys_2p25", "n": n, "bytes_per_key": 12, "runs": res}
 
 
+def run_long64(dev, peak_gbs: float) -> dict:
+    """int64 positions beyond 2^31 keys: N = 2^32 int32 keys through
+    Plan.run64 on a plan of the largest capacity (two pieces), uniform and
+    strictly descending over the whole int32 range; device time with L2
+    flushed; useful bytes 12 per key (4 in, 8 out)."""
+    import torch
+
+    from apsep_gb300 import Plan, _lib
+
+    n = 1 << 32
+    plan = Plan(_lib.MAX_KEYS, torch.int32, device=dev, tuning=None)
+    work = torch.empty(plan.workspace64_bytes(n), dtype=torch.uint8, device=dev)
+    out = torch.empty(n, dtype=torch.int64, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g = torch.Generator(device=dev)
+    g.manual_seed(43)
+    res = {}
+    for name in ("uniform", "descending"):
+        if name == "uniform":
+            x = torch.randint(0, (1 << 31) - 1, (n,), generator=g, device=dev, dtype=torch.int32)
+        else:
+            x = (torch.arange(n - 1, -1, -1, device=dev, dtype=torch.int64) - (1 << 31)).to(torch.int32)
+        for _ in range(2):
+            plan.run64(x, out=out, work=work)
+        ts = []
+        for _ in range(5):
+            flush_l2(flush)
+            e0.record()
+            plan.run64(x, out=out, work=work)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
+        plan.check()
+        ms = statistics.median(ts)
+        gbs = 12.0 * n / ms / 1e6
+        res[name] = {"ms": round(ms, 2), "gbs": round(gbs, 1), "frac": round(gbs / peak_gbs, 4)}
+        del x
+    plan.close()
+    del out, work
+    return {"workload": "positions64_2p32_int32", "n": n, "pieces": 2, "bytes_per_key": 12, "runs": res}
+
+
 def run_served(dev) -> dict:
     from apsep_gb300.serve import Server, plain_loop
     from apsep_gb300.workloads import serve_requests
@@ -666,6 +712,8 @@ def run_ours(args) -> None:
         line["consumers"] = run_consumers(dev, peaks["hbm_gbs"])
         torch.cuda.empty_cache()
         line["wide"] = run_wide(dev, peaks["hbm_gbs"])
+        torch.cuda.empty_cache()
+        line["long64"] = run_long64(dev, peaks["hbm_gbs"])
         torch.cuda.empty_cache()
         line["sweep"] = run_sweep(dev, peaks["hbm_gbs"])
     print(json.dumps(line), flush=True)
