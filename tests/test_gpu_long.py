@@ -80,6 +80,27 @@ def test_pieces_against_the_oracle(plans, name, dtype):
                             % (cap, n, le, bad, got[bad], want[bad]))
 
 
+@pytest.mark.parametrize("dtype", TYPES, ids=lambda t: t.__name__)
+def test_pieces_off_a_16_byte_boundary(plans, dtype):
+    # keys one element past an aligned base: 4-byte keys run each piece behind
+    # a view head (level-1 minima then come from the keys themselves), 8-byte
+    # keys without TMA; answers to an 8-byte aligned int64 buffer
+    rng = np.random.default_rng(90 + TYPES.index(dtype))
+    n = 60_007
+    for name in ("uniform", "rising_runs", "walk"):
+        a = keys(name, n, rng, dtype, 992)
+        base = torch.zeros(n + 1, dtype=torch.from_numpy(a[:0]).dtype, device="cuda")
+        base[1:] = torch.from_numpy(a).cuda()
+        ob = torch.full((n + 2,), -7, dtype=torch.int64, device="cuda")
+        for le in (False, True):
+            plan = plans(dtype, 1000)
+            plan.run64(base[1:], out=ob[1:n + 1], inclusive=le)
+            plan.check()
+            got = ob.cpu().numpy()
+            assert got[0] == -7 and got[n + 1] == -7
+            assert np.array_equal(got[1:n + 1], oracle.apse(a, le).astype(np.int64)), (name, le)
+
+
 def test_one_piece_matches_the_int32_run(plans):
     rng = np.random.default_rng(7)
     plan = plans(np.int32, 300_000)
