@@ -12,9 +12,23 @@
 // threads over the five scratch arrays of allocSPTScratch
 // (src/apsep.cuh:3014-3040).  Its float path converts keys by value
 // (src/apsep.cuh:2689-2690), so only int32 keys are instantiated.
+//
+// Also the reference's generic multi-kernel path, WSTL (strict comparator,
+// src/apsep.cuh:2296-2500, driven by runWSTL, src/apsep.cuh:2548-2596): its
+// four kernels for int32 and float32 keys, the reference's own GPU oracle for
+// float keys.
 #include "apsep.cuh"
 
 template __global__ void apsepKernelSPT<int, 128, 4, false>(const int*, int*, int, int, int, int, unsigned*, int*,
                                                             int*, int*, int*);
 template __global__ void apsepKernelSPT<int, 128, 4, true>(const int*, int*, int, int, int, int, unsigned*, int*,
                                                            int*, int*, int*);
+
+#define APSEP_REF_WSTL(T)                                                                                      \
+    template __global__ void wstlPass1Kernel<T, 128, 4>(const T*, int*, int, int, T*, T*, T*);                \
+    template __global__ void wstlFillLeavesKernel<T>(const T*, T*, int, int, int);                            \
+    template __global__ void wstlReduceLevelKernel<T>(T*, int, int);                                          \
+    template __global__ void wstlPass3Kernel<T, 128, 4>(const T*, int*, int, int, const T*, const T*, const T*, \
+                                                        const T*, int);
+APSEP_REF_WSTL(int)
+APSEP_REF_WSTL(float)
