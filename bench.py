@@ -54,6 +54,8 @@ Extra objects on the same line (one GPU only; --no-extras skips them):
   long64     int64 positions beyond 2^31 keys (Plan.run64): N = 2^32 int32
              keys in two pieces of 2^31 - 4096, uniform and descending; time,
              useful GB/s (12 B/key: 4 in, 8 out) and fraction of peak.
+  le         the previous-smaller-or-equal comparator (INCL=true) at
+             N = 2^25, the four distributions: time, GB/s, fraction.
   sweep      single-array useful GB/s and roofline fraction for N = 2^14 ..
              2^30 (every second power of two), uniform and descending keys.
 
@@ -371,6 +373,38 @@ def run_wide(dev, peak_gbs: float) -> dict:
     for p in plans.values():
         p.close()
     return {"workload": "wide_keys_2p25", "n": n, "bytes_per_key": 12, "runs": res}
+
+
+def run_le(dev, peak_gbs: float) -> dict:
+    """The previous-smaller-or-equal comparator (the reference's INCL=true,
+    src/apsep.cuh:2669-2673) on the headline workload: N = 2^25 int32, the
+    same four distributions, device time with L2 flushed, 8 useful B/key."""
+    import torch
+
+    from apsep_gb300 import Plan
+
+    xs = {k: torch.from_numpy(v).to(dev) for k, v in make_inputs().items()}
+    out = torch.empty(N, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res = {}
+    with Plan(N, torch.int32, inclusive=True, device=dev) as plan:
+        for name, x in xs.items():
+            for _ in range(3):
+                plan.run(x, out=out)
+            ts = []
+            for _ in range(9):
+                flush_l2(flush)
+                e0.record()
+                plan.run(x, out=out)
+                e1.record()
+                torch.cuda.synchronize(dev)
+                ts.append(e0.elapsed_time(e1))
+            plan.check()
+            ms = statistics.median(ts)
+            gbs = 8.0 * N / ms / 1e6
+            res[name] = {"us": round(ms * 1e3, 1), "gbs": round(gbs, 1), "frac": round(gbs / peak_gbs, 4)}
+    return {"workload": "apse_le_2p25_int32", "n": N, "bytes_per_key": 8, "runs": res}
 
 
 def run_long64(dev, peak_gbs: float) -> dict:
@@ -714,6 +748,8 @@ def run_ours(args) -> None:
         line["wide"] = run_wide(dev, peaks["hbm_gbs"])
         torch.cuda.empty_cache()
         line["long64"] = run_long64(dev, peaks["hbm_gbs"])
+        torch.cuda.empty_cache()
+        line["le"] = run_le(dev, peaks["hbm_gbs"])
         torch.cuda.empty_cache()
         line["sweep"] = run_sweep(dev, peaks["hbm_gbs"])
     print(json.dumps(line), flush=True)
