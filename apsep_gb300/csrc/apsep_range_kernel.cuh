@@ -650,14 +650,26 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 }
             }
 
-            // ---- a whole tile above the stack top (strict comparator) -----------------------
+            // ---- a whole tile above the stack top ---------------------------------------------
             // A strictly increasing tile whose first key is above the stack's top entry
-            // (the range's last key): every key answers its predecessor, every key is a
-            // strict suffix minimum, and the ring keeps the tile's last K keys.
-            if constexpr (EP && !INCL) {  // (strict comparator: adj means strictly increasing)
+            // (the range's last key): every key answers its predecessor under either
+            // comparator, every key is a strict suffix minimum, and the ring keeps the
+            // tile's last K keys.
+            if constexpr (EP) {
                 const T first = __shfl_sync(FULL, v[0], 0);
-                if (mono == FULL && valid_keys == WT && __all_sync(FULL, adj && b_adj) && stk_hi > stk_lo &&
-                    sStkV[(stk_hi - 1) & (K - 1)] < first) {
+                bool up = mono == FULL && valid_keys == WT && __all_sync(FULL, adj && b_adj) && stk_hi > stk_lo &&
+                          sStkV[(stk_hi - 1) & (K - 1)] < first;
+                if constexpr (INCL) {
+                    // adj means non-decreasing here: ties would not all be strict suffix
+                    // minima, so check strict increase (only on such tiles)
+                    if (up) {
+                        bool inc = lane == 0 || prev_last < v[0];
+#pragma unroll
+                        for (int k = 1; k < IPT; k++) inc = inc && v[k - 1] < v[k];
+                        up = __all_sync(FULL, inc);
+                    }
+                }
+                if (up) {
                     // answers relative to the array (a view head's pads are never the
                     // stack top here: a pad does not lie below the tile's first key)
                     const int top_pos = sStkP[(stk_hi - 1) & (K - 1)] - head;
