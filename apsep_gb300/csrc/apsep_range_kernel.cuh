@@ -379,7 +379,7 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
 // MAPF: int64 key slots that hold float64 bit patterns, compared through
 // f64_order (keys are mapped as they enter shared memory or registers).
 template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false>
-__global__ void __launch_bounds__(WPC * 32, (sizeof(T) == 8 ? 2 : IPT >= 16 ? (WPC >= 16 ? 1 : 2) : 3))
+__global__ void __launch_bounds__(WPC * 32, (WPC >= 16 && sizeof(T) == 4 ? 1 : 2))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
     constexpr int KB = (int)sizeof(T);  // bytes per key
