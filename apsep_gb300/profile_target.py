@@ -3,9 +3,13 @@
     python -m apsep_gb300.profile_target [--dist uniform|descending|ascending|dup16]
                                          [--n 33554432] [--reps 3] [--config 0]
                                          [--dtype int32|float32|int64|float64]
+                                         [--piece KEYS]
 
 Allocates one input and one output ((4 or 8) * n + 4 * n bytes), runs `reps` APSE
 launches with a synchronisation after each, prints the last launch's time.
+With --piece, each rep is one Plan.run64 (int64 positions, 8 * n bytes of
+answers) on a plan of that capacity, so the array runs as pieces of that
+many keys (engine run + widening pass per piece).
 Small enough on the device for ncu captures; n = 2^25 keeps the 128 MiB
 input above the 126 MiB L2.
 """
@@ -26,6 +30,7 @@ def main() -> None:
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--config", type=int, default=0)
     ap.add_argument("--dtype", default="int32", choices=("int32", "float32", "int64", "float64"))
+    ap.add_argument("--piece", type=int, default=0)
     a = ap.parse_args()
     rng = np.random.default_rng(7)
     n = a.n
@@ -39,8 +44,19 @@ def main() -> None:
         h = rng.integers(0, 16, n)
     dt = getattr(torch, a.dtype)
     x = torch.from_numpy(h.astype(getattr(np, a.dtype))).cuda()
-    out = torch.empty(n, dtype=torch.int32, device="cuda")
-    plan = Plan(n, dt)
+    if a.piece:
+        plan = Plan(a.piece, dt, tuning=None)
+        out = torch.empty(n, dtype=torch.int64, device="cuda")
+        work = torch.empty(max(plan.workspace64_bytes(n), 16), dtype=torch.uint8, device="cuda")
+
+        def run():
+            plan.run64(x, out=out, work=work)
+    else:
+        out = torch.empty(n, dtype=torch.int32, device="cuda")
+        plan = Plan(n, dt)
+
+        def run():
+            plan.run(x, out=out)
     if dt in (torch.int32, torch.float32):
         plan.set_config(a.config)  # (8-byte keys have one configuration)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -48,7 +64,7 @@ def main() -> None:
     for _ in range(a.reps):
         torch.cuda._sleep(200000)  # keep the stream busy so launch overhead stays off the clock
         e0.record()
-        plan.run(x, out=out)
+        run()
         e1.record()
         plan.check()
         times.append(e0.elapsed_time(e1) * 1e3)
@@ -56,7 +72,7 @@ def main() -> None:
     med = t[len(t) // 2]
     kb = x.element_size()
     print("done dist=%s dtype=%s n=%d median=%.1f us min=%.1f max=%.1f (%.1f GB/s useful at the median)"
-          % (a.dist, a.dtype, n, med, t[0], t[-1], (kb + 4.0) * n / (med * 1e-6) / 1e9))
+          % (a.dist, a.dtype, n, med, t[0], t[-1], (kb + out.element_size()) * n / (med * 1e-6) / 1e9))
     plan.close()
 
 
