@@ -585,14 +585,31 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             const int nvalid = min(max(a.n - lb, 0), IPT);
             // Monotone lanes: each key answers its neighbour (adj), or no key answers
             // any later one (none); across the lane boundary likewise (b_adj, b_none).
-            bool adj = true, none = true;
+            // A few neighbour pairs first: on almost every tile of unordered keys some
+            // lane is already neither increasing nor non-increasing there, and the
+            // full check (15 compares a lane) is skipped.
+            bool adj = false, none = false;
+            unsigned mono = 0u;
+            {
+                bool qa = true, qn = true;
 #pragma unroll
-            for (int k = 1; k < IPT; k++) {
-                const bool l = lt<INCL>(v[k - 1], v[k]);
-                adj = adj && l;
-                none = none && !l;
+                for (int k = IPT / 4; k < IPT; k += IPT / 4) {
+                    const bool l = lt<INCL>(v[k - 1], v[k]);
+                    qa = qa && l;
+                    qn = qn && !l;
+                }
+                if (__all_sync(FULL, qa || qn)) {
+                    adj = true;
+                    none = true;
+#pragma unroll
+                    for (int k = 1; k < IPT; k++) {
+                        const bool l = lt<INCL>(v[k - 1], v[k]);
+                        adj = adj && l;
+                        none = none && !l;
+                    }
+                    mono = __ballot_sync(FULL, adj || none);
+                }
             }
-            const unsigned mono = __ballot_sync(FULL, adj || none);
             const T prev_last = __shfl_up_sync(FULL, v[IPT - 1], 1);
             const bool b_adj = lane == 0 || lt<INCL>(prev_last, v[0]);
 
@@ -743,7 +760,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 }
 #pragma unroll
                 for (int k = 0; k < IPT; k++)
-                    if (res[k] < 0 && k < nvalid) umask |= 1u << k;
+                    if (res[k] < 0) umask |= 1u << k;
+                if (nvalid < IPT) umask &= (1u << nvalid) - 1u;  // (the tail tile's pads)
                 // in-thread answers; every other key holds -1 until resolved below
 #pragma unroll
                 for (int q4 = 0; q4 < IPT / 4; q4++)
@@ -793,11 +811,16 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             // ---- 3. classify the keys without an in-thread answer ------------------------
             // X: answered by an earlier lane of the tile; S: by an earlier tile of the
             // range (the stack); D: by nothing in the range (deferred to phase 2).
-            unsigned gtb = 0, gtr = 0;
+            unsigned gtb = 0, gtr = ~0u;
 #pragma unroll
-            for (int k = 0; k < IPT; k++) {
-                gtb |= (unsigned)lt<INCL>(before, v[k]) << k;
-                gtr |= (unsigned)lt<INCL>(rmin, v[k]) << k;
+            for (int k = 0; k < IPT; k++) gtb |= (unsigned)lt<INCL>(before, v[k]) << k;
+            // Every key of a lane is >= the lane minimum: when the range minimum
+            // qualifies for every lane's minimum (most tiles after a range's first),
+            // it qualifies for every key and the per-key compares are skipped.
+            if (!__all_sync(FULL, lt<INCL>(rmin, lmin))) {
+                gtr = 0u;
+#pragma unroll
+                for (int k = 0; k < IPT; k++) gtr |= (unsigned)lt<INCL>(rmin, v[k]) << k;
             }
             const unsigned xm = lane > 0 ? (umask & gtb) : 0u;
             const unsigned sm = has_rmin ? (umask & ~xm & gtr) : 0u;
