@@ -126,6 +126,42 @@ def test_edge_sizes_vs_oracle(plans, name, le):
                                                                                want[bad]))
 
 
+def near_monotone(n, kind, ipt):
+    """Keys that pass a check of a few neighbour pairs per lane (pairs ending at
+    k = ipt/4, ipt/2, 3*ipt/4 of each lane's ipt keys) but are not monotone:
+    one dip (or bump) at k = 1 of every lane; and monotone runs with ties."""
+    i = np.arange(n, dtype=np.int64)
+    if kind == "asc_dip":
+        a = i * 4
+        a[i % ipt == 1] -= 10
+    elif kind == "desc_bump":
+        a = -i * 4
+        a[i % ipt == 1] += 10
+    elif kind == "asc_ties":  # non-decreasing: ties every 1000 keys and at every lane start
+        a = i - i // 1000
+        a[i % 97 == 0] = a[np.maximum(i[i % 97 == 0] - 1, 0)]
+    else:  # strictly increasing tiles, one tile in 50 with a tie
+        a = i * 2
+        a[(i % (50 * 512)) == 300] -= 2
+    return a.astype(np.int32)
+
+
+@pytest.mark.parametrize("config", [0, 1])
+@pytest.mark.parametrize("kind", ["asc_dip", "desc_bump", "asc_ties", "asc_rare_tie"])
+@pytest.mark.parametrize("le", [False, True])
+def test_near_monotone_tiles(config, kind, le):
+    ipt = 16 if config == 0 else 8
+    n = 3_000_017
+    a = near_monotone(n, kind, ipt)
+    with Plan(n, torch.int32, inclusive=le, tuning=None) as plan:
+        plan.set_config(config)
+        got = run_gpu(plan, a, le=le)
+    want = oracle.apse(a, le)
+    if not np.array_equal(got, want):
+        bad = int(np.flatnonzero(got != want)[0])
+        pytest.fail("first mismatch at %d: got %d want %d" % (bad, got[bad], want[bad]))
+
+
 @pytest.mark.parametrize("config", [0, 1])
 def test_every_config(config):
     rng = np.random.default_rng(77 + config)
