@@ -204,8 +204,8 @@ apsep_status apsep_cartesian_parents(apsep_plan* plan, const void* d_in, int32_t
  * piece.  d_work: a 16-byte aligned device workspace of
  * apsep_run64_workspace_bytes(plan, n) bytes (-1: n out of range, or a plan
  * with capacity < 32 for n > capacity), not overlapping the keys or d_out
- * (8-byte aligned).  Asynchronous on `stream`; device-side errors surface
- * through apsep_plan_check. */
+ * (8-byte aligned).  Asynchronous on `stream` and graph-capturable like
+ * apsep_run; device-side errors surface through apsep_plan_check. */
 #define APSEP_MAX_KEYS64 1099511627776LL /* 2^40 */
 int64_t apsep_run64_workspace_bytes(const apsep_plan* plan, int64_t n);
 apsep_status apsep_run64(apsep_plan* plan, const void* d_in, int64_t* d_out, int64_t n, apsep_cmp cmp,

@@ -242,3 +242,31 @@ def test_beyond_2p31_keys_ascending():
         assert torch.equal(out[lo:hi], torch.arange(lo - 1, hi - 1, dtype=torch.int64, device="cuda"))
     del out, x
     torch.cuda.empty_cache()
+
+
+def test_graph_capture_of_pieces(plans):
+    # every piece's engine run, widening pass and level build replay from one graph
+    plan = plans(np.int32, 1000)
+    n = 60_007
+    rng = np.random.default_rng(21)
+    x = torch.empty(n, dtype=torch.int32, device="cuda")
+    out = torch.empty(n, dtype=torch.int64, device="cuda")
+    work = torch.empty(plan.workspace64_bytes(n), dtype=torch.uint8, device="cuda")
+    x.copy_(torch.from_numpy(keys("walk", n, rng, np.int32, 992)))
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        plan.run64(x, out=out, work=work)  # warm-up outside capture
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.run64(x, out=out, work=work)
+    for name in ("uniform", "rising_runs", "desc", "walk"):
+        a = keys(name, n, rng, np.int32, 992)
+        x.copy_(torch.from_numpy(a))
+        out.fill_(-7)
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), oracle.apse(a).astype(np.int64)), name
+    plan.check()
