@@ -1,11 +1,12 @@
 // apsep_range_kernel.cuh -- the APSE engine for sm_103a: persistent,
 // warp-independent ranges (single arrays and batches of segments).
 //
-// One launch.  Every WARP is an independent worker: it claims a contiguous
-// RANGE of warp tiles (32 lanes x IPT keys) from an atomic counter, keeps its
-// own ring of TMA stages, its own answer buffers and its own stack in shared
-// memory, and synchronises only with __syncwarp -- there is no CTA-wide
-// barrier anywhere.
+// One launch.  Every WARP is an independent worker on a contiguous RANGE of
+// warp tiles (32 lanes x IPT keys; the first warp of each CTA claims the
+// CTA's consecutive ranges with one atomic, in CTA start order), with its own
+// ring of TMA stages, its own answer buffers and its own stack in shared
+// memory.  One __syncthreads publishes the claim; after it the warps
+// synchronise only with __syncwarp.
 //
 //  Phase 1, per warp tile (the next tiles' 128-byte-swizzled TMA loads stay
 //  in flight in the warp's ring):
@@ -20,8 +21,9 @@
 //      binary search over that lane's suffix minima -- a fixed number of
 //      steps in place of the reference's warp-uniform pointer jumping, spine
 //      walk and cross-warp fallback (src/apsep.cuh:2734-2801);
-//   5. S keys binary-search the warp's RANGE STACK (strict suffix minima of
-//      the range's earlier tiles), in place of the reference's global
+//   5. S keys search the warp's RANGE STACK (strict suffix minima of the
+//      range's earlier tiles; its top 32 entries one per lane, a shuffle
+//      search, binary search below), in place of the reference's global
 //      min-tree descent (src/apsep.cuh:2952-2996) for every answer inside the
 //      range;
 //   6. the whole tile leaves shared memory in one TMA store, deferred keys as
@@ -46,7 +48,7 @@ namespace apsep {
 
 constexpr int kStages = 3;      // TMA ring depth per warp (tiles)
 constexpr int kStackCap = 64;   // range-stack entries kept per warp
-constexpr int kXQueries = 3;    // cross-lane queries per lane and round (32 * 4 keys per round)
+constexpr int kXQueries = 3;    // cross-lane queries per lane and round (32 * 3 keys per round)
 constexpr int kDefCap = 64;     // deferred keys listed in shared memory per range
 constexpr int kCapCap = 16;     // capped keys listed in shared memory per range
 
