@@ -18,6 +18,9 @@ beside it.
   per_distribution  median (with p10 / p90) device time per distribution,
              and the median of the same steps back to back without the
              flush.
+  reference_published  the reference's published SPT figures at N = 2^25
+             (one GTX 1660 Ti, per distribution) and ours over them:
+             context only, other hardware.
   e2e        the same metric through the public API with host buffers: each
              step copies the keys from pinned host memory, runs, and copies
              the answers back, all inside the timed region.  value: the steps
@@ -712,6 +715,13 @@ def run_ours(args) -> None:
     traffic = profile_traffic()
     for name in per:
         per[name]["frac"] = round(per[name]["gbs"] / peaks["hbm_gbs"], 4)
+    # The reference's only published numbers for this metric: SPT at N = 2^25 on one
+    # GTX 1660 Ti (README.md:27-29), per distribution; other hardware, so context
+    # only (vs_baseline stays null: no published figure for this aggregate on GB300).
+    published = {"uniform": 98.2, "descending": 181.7, "ascending": 174.4}
+    reference_published = {"hardware": "GTX 1660 Ti (288 GB/s)", "gbs": published,
+                           "ours_over_published": {k: round(per[k]["gbs"] / v, 1)
+                                                   for k, v in published.items() if k in per}}
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5), "higher_is_better": True,
@@ -720,6 +730,7 @@ def run_ours(args) -> None:
                    "l2": "flushed before every step (512 MiB written then read, outside the timed events)",
                    "parallelism": "replicas x%d" % world},
         "per_distribution": per,
+        "reference_published": reference_published,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
