@@ -164,6 +164,14 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
 
+    def wait_ready(self, timeout: float = 5.0) -> None:
+        """Until the first sample arrives: nvidia-smi's start-up (driver
+        attach) then lies outside the timed region, where it would stall a
+        launch and stretch that step's event time."""
+        t_end = time.time() + timeout
+        while self.proc is not None and not self.samples and time.time() < t_end:
+            time.sleep(0.01)
+
     def mark(self, t0, t1):
         self.window = (t0, t1)
 
@@ -638,7 +646,10 @@ def run_ours(args) -> None:
     sampler = ClockSampler(local)
     if rank == 0:
         sampler.start()
-        time.sleep(0.3)
+        sampler.wait_ready()
+        time.sleep(0.2)
+    flush_l2(flush)  # one more untimed step once the sampler runs
+    plan.run(d_in[DISTS[0]], out=out)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if dist:
         dist.barrier()
