@@ -30,6 +30,7 @@ SIGNATURES = {
     "apsep_launch": ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "apsep_debug_inject": ([_vp, _i32, _u32], ctypes.c_int),
     "apsep_run_noalloc": ([_vp, _vp, _i64, ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
+    "apsep_noalloc_check": ([_vp], ctypes.c_int),
     "apsep_run_segmented": ([_vp, _vp, _vp, _i64, _vp, _i32, _vp], ctypes.c_int),
     "apsep_consumer_workspace_bytes": ([_i64], _i64),
     "apsep_run_prev_greater": ([_vp, _vp, _vp, _i64, ctypes.c_int, _vp, _vp], ctypes.c_int),

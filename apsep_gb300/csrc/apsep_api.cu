@@ -354,7 +354,11 @@ apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dty
 }
 
 apsep_status apsep_debug_inject(apsep_plan* p, int32_t range, uint32_t spin_limit) {
-    if (!p || range < -1) return APSEP_EINVAL;
+    if (range < -1) return APSEP_EINVAL;
+    if (!p) {  // the next apsep_run_noalloc call
+        noalloc_debug_inject(range, spin_limit);
+        return APSEP_OK;
+    }
     p->dbg_skip_range = range;
     p->dbg_spin_limit = spin_limit;
     return APSEP_OK;

@@ -153,6 +153,8 @@ cudaError_t launch_range_view(int dtype, int incl, int cfg, RangeArgs& a, const 
                               const CUtensorMap& map_out, cudaStream_t st);
 cudaError_t prepare_segmented(int cfg, int* ctas_per_sm);
 cudaError_t range_max_warps(int cfg, int* warps);  // persistent warps of one launch, current device
+// Arms one-shot fault injection for the next apsep_run_noalloc call.
+void noalloc_debug_inject(int32_t range, uint32_t spin_limit);
 
 }  // namespace apsep
 

@@ -11,11 +11,16 @@
 // that array (2,869,504 bytes) until the process exits.
 //
 // Host code must not pass the array's name to a kernel: on the host it is
-// only a stand-in symbol.  The first call on each device looks up the
-// array's device address with cudaGetSymbolAddress (with that device
-// current) and initialises its control block; later calls reuse the
-// address.  All calls share the one array, so calls whose kernels overlap on
-// the GPU race and must be serialised by the caller (e.g. one stream).
+// only a stand-in symbol.  Every call looks up the array's device address
+// with cudaGetSymbolAddress (with the caller's device current; the lookup
+// allocates nothing).  The first call in each CUDA context on a device -- the
+// first of the process, or the first after cudaDeviceReset or a switch to
+// another context, each of which loads the module afresh -- clears the array
+// and writes its initial control block.  All calls share the one array, so
+// calls whose kernels overlap on the GPU race and must be serialised by the
+// caller (e.g. one stream).  Device-side errors (a wait that gave up, a
+// broken search invariant) are sticky in the array's control block until
+// apsep_noalloc_check reads and clears them.
 #include <cudaTypedefs.h>
 #include <string.h>
 
@@ -40,7 +45,36 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
 std::mutex g_mu;
+// Per device: the context whose copy of the array was last set up, and its address.
+unsigned long long g_ctx[kMaxDevices] = {};
 void* g_addr[kMaxDevices] = {};
+// One-shot fault injection for the next run (apsep_debug_inject with no plan).
+int g_dbg_skip_range = -1;
+uint32_t g_dbg_spin_limit = 0;
+
+using PFN_ctxGetCurrent = CUresult (*)(CUcontext*);
+using PFN_ctxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the caller's current CUDA context (0 if none can be read).
+unsigned long long current_context_id() {
+    static PFN_ctxGetCurrent get_cur = nullptr;
+    static PFN_ctxGetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = (PFN_ctxGetCurrent)p;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (PFN_ctxGetId)p;
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_cur || !get_id || get_cur(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 PFN_cuTensorMapEncodeTiled_v12000 encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -69,19 +103,28 @@ bool encode(CUtensorMap* map, const void* base, int rows, int tile_rows, int dty
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Device address of the static scratch on the current device; the first
-// call per device resolves it and writes the initial control block.
+// Device address of the static scratch on the current device and context.
+// The address is looked up on every call; the array is set up when the
+// context (or the address) differs from the one set up last on this device.
 apsep_status scratch_for_current_device(void** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return APSEP_ECUDA;
     if (dev < 0 || dev >= kMaxDevices) return APSEP_ENOTSUP;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-            cudaGetLastError();
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return APSEP_ECUDA;
+    }
+    const unsigned long long ctx = current_context_id();
+    if (g_addr[dev] != p || g_ctx[dev] != ctx) {
+        int major = 0;
+        if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess)
             return APSEP_ECUDA;
-        }
+        if (major < 10) return APSEP_ENOTSUP;  // the engine is built for sm_103a
+        // Stale tags from runs in an earlier context could alias the restarted
+        // epochs: clear the whole array, then write the initial control block.
+        if (cudaMemset(p, 0, kBytes) != cudaSuccess) return APSEP_ECUDA;
         Counters c0;
         memset(&c0, 0, sizeof(c0));
         c0.epoch = 1;
@@ -91,8 +134,9 @@ apsep_status scratch_for_current_device(void** out) {
         if (cudaMemset(rs0.group_min, 0xff, group_min_bytes()) != cudaSuccess) return APSEP_ECUDA;
         if (range_prepare(kConfig) != cudaSuccess) return APSEP_ECUDA;
         g_addr[dev] = p;
+        g_ctx[dev] = ctx;
     }
-    *out = g_addr[dev];
+    *out = p;
     return APSEP_OK;
 }
 
@@ -147,11 +191,43 @@ extern "C" apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int6
     a.tiles_per_range = 0;
     a.num_ranges = 0;
     a.tma_rows = rows;
-    a.spin_limit = kSpinLimit;
-    a.skip_publish_range = -1;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        a.spin_limit = g_dbg_spin_limit ? g_dbg_spin_limit : kSpinLimit;
+        a.skip_publish_range = g_dbg_skip_range;
+        g_dbg_skip_range = -1;  // one-shot
+        g_dbg_spin_limit = 0;
+    }
     a.s = rs;
     const int incl = cmp == APSEP_LE ? 1 : 0;
     cudaError_t e = head ? launch_range_view(dtype, incl, kConfig, a, mi, mo, (cudaStream_t)stream)
                          : launch_range(dtype, incl, kConfig, a, mi, mo, (cudaStream_t)stream);
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }
+
+extern "C" apsep_status apsep_noalloc_check(void* stream) {
+    void* base = nullptr;
+    apsep_status st = scratch_for_current_device(&base);
+    if (st != APSEP_OK) return st;
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return APSEP_ECUDA;
+    Counters c0;
+    if (cudaMemcpy(&c0, base, sizeof(c0), cudaMemcpyDeviceToHost) != cudaSuccess) return APSEP_ECUDA;
+    const uint32_t err = c0.err;
+    if (!err) return APSEP_OK;
+    // A run that gave up may have left its counters half-way: re-arm the
+    // control block, keeping the epoch.
+    const uint32_t epoch = c0.epoch;
+    memset(&c0, 0, sizeof(c0));
+    c0.epoch = epoch;
+    if (cudaMemcpy(base, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) return APSEP_ECUDA;
+    if (err & (ERR_LOOKBACK_TIMEOUT | ERR_TMA_TIMEOUT)) return APSEP_ETIMEOUT;
+    return APSEP_EINTERNAL;
+}
+
+namespace apsep {
+void noalloc_debug_inject(int32_t range, uint32_t spin_limit) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_dbg_skip_range = range;
+    g_dbg_spin_limit = spin_limit;
+}
+}  // namespace apsep

@@ -145,13 +145,25 @@ apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dty
  * every entry point allocates or takes caller-allocated scratch.
  * The scratch is a static device array sized for APSEP_NOALLOC_MAX_KEYS keys
  * (2,869,504 bytes, held on every GPU that loads the library until exit);
- * n > APSEP_NOALLOC_MAX_KEYS returns APSEP_EINVAL.  The first call on each
- * device resolves the array's address and initialises it, so make that
- * first call before any stream capture.  All calls share the array: calls
- * whose kernels overlap on the GPU race, so serialise them (e.g. one
- * stream).  Asynchronous on `stream`; device-side errors are not reported. */
+ * n > APSEP_NOALLOC_MAX_KEYS returns APSEP_EINVAL; a device below compute
+ * capability 10 returns APSEP_ENOTSUP.  Every call looks up the array's
+ * address (a lookup that allocates nothing); the first call in each CUDA
+ * context on a device -- the first of the process, and the first after
+ * cudaDeviceReset or a switch to another context -- clears the array and
+ * initialises it, so make that first call before any stream capture.  All
+ * calls share the array: calls whose kernels overlap on the GPU race, so
+ * serialise them (e.g. one stream).  Asynchronous on `stream`; device-side
+ * errors stay in the array until apsep_noalloc_check reads them. */
 apsep_status apsep_run_noalloc(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp,
                                void* stream);
+
+/* The device-side error state of apsep_run_noalloc on the current device
+ * (the counterpart of apsep_plan_check, and like it no counterpart in the
+ * reference): synchronises `stream`, then returns APSEP_ETIMEOUT if a wait
+ * of an earlier run gave up, APSEP_EINTERNAL if a search invariant failed,
+ * else APSEP_OK, and clears the error (the answers of a run that reported
+ * one are not valid).  Allocates nothing. */
+apsep_status apsep_noalloc_check(void* stream);
 
 /* ---- Consumers of APSE ------------------------------------------------------
  * The classic callers the reference names for its output (README.md:3,
@@ -212,11 +224,12 @@ apsep_status apsep_run64(apsep_plan* plan, const void* d_in, int64_t* d_out, int
                          void* d_work, void* stream);
 
 /* Fault injection for failure-detection tests: in the next run, range `range`
- * (the contiguous block of tiles one persistent CTA sweeps) never publishes
+ * (the contiguous block of tiles one persistent warp sweeps) never publishes
  * its look-back status, and every device wait gives up after `spin_limit`
  * polls, so its successors report APSEP_ETIMEOUT through apsep_plan_check
  * instead of hanging.  range = -1 restores normal runs (spin_limit 0 =
- * default). */
+ * default).  plan = NULL arms the next apsep_run_noalloc call instead
+ * (reported by apsep_noalloc_check). */
 apsep_status apsep_debug_inject(apsep_plan* plan, int32_t range, uint32_t spin_limit);
 
 #ifdef __cplusplus

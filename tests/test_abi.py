@@ -66,7 +66,8 @@ def test_argument_validation_without_device(built_lib):
     assert lib.apsep_plan_destroy(None) == _lib.APSEP_OK
     assert lib.apsep_plan_check(None, None) == _lib.APSEP_EINVAL
     assert lib.apsep_plan_set_config(None, 0) == _lib.APSEP_EINVAL
-    assert lib.apsep_debug_inject(None, 0, 0) == _lib.APSEP_EINVAL
+    assert lib.apsep_debug_inject(None, -2, 0) == _lib.APSEP_EINVAL
+    assert lib.apsep_debug_inject(None, -1, 0) == _lib.APSEP_OK  # (no plan: the no-alloc path, disarmed)
     assert lib.apsep_launch(None, None, 0, 0, 0) == _lib.APSEP_OK  # n == 0 is a no-op
     assert lib.apsep_run64_workspace_bytes(None, 10) == -1
     assert lib.apsep_run64(None, None, None, 5, 0, None, None) == _lib.APSEP_EINVAL
