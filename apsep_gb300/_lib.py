@@ -23,6 +23,8 @@ SIGNATURES = {
     "apsep_run": ([_vp, _vp, _vp, _i64, _vp], ctypes.c_int),
     "apsep_run_cmp": ([_vp, _vp, _vp, _i64, ctypes.c_int, _vp], ctypes.c_int),
     "apsep_plan_check": ([_vp, _vp], ctypes.c_int),
+    "apsep_plan_error_async": ([_vp, _vp, _vp], ctypes.c_int),
+    "apsep_copy_spans": ([_vp, _vp, _vp, _i32, _vp], ctypes.c_int),
     "apsep_plan_get_info": ([_vp, _vp], ctypes.c_int),
     "apsep_plan_set_config": ([_vp, _i32], ctypes.c_int),
     "apsep_num_configs": ([], _i32),
@@ -96,3 +98,14 @@ def status_string(status: int) -> str:
 def check(status: int, what: str = "") -> None:
     if status != APSEP_OK:
         raise ApsepError(status, what)
+
+
+def copy_spans(srcs, dsts, nbytes, stream_handle: int) -> None:
+    """apsep_copy_spans over Python lists of addresses and byte counts."""
+    n = len(srcs)
+    if n == 0:
+        return
+    a = (ctypes.c_void_p * n)(*srcs)
+    b = (ctypes.c_void_p * n)(*dsts)
+    c = (ctypes.c_int64 * n)(*nbytes)
+    check(load().apsep_copy_spans(a, b, c, n, ctypes.c_void_p(stream_handle)), "apsep_copy_spans")

@@ -163,6 +163,16 @@ class Plan:
         _lib.check(self._lib.apsep_plan_check(self._h, ctypes.c_void_p(_stream_handle(self.device, stream))),
                    "apsep_plan_check")
 
+    def error_async(self, host_word: torch.Tensor, stream=None) -> None:
+        """Enqueue a copy of the plan's device-side error word into host_word
+        (a pinned int32 host tensor of >= 1 element); nonzero once the stream
+        has passed the copy means an earlier run failed (decode with check())."""
+        if host_word.is_cuda or host_word.dtype != torch.int32 or host_word.numel() < 1:
+            raise ValueError("host_word must be a pinned host int32 tensor")
+        _lib.check(self._lib.apsep_plan_error_async(self._h, ctypes.c_void_p(host_word.data_ptr()),
+                                                    ctypes.c_void_p(_stream_handle(self.device, stream))),
+                   "apsep_plan_error_async")
+
     def debug_inject(self, range_index: int, spin_limit: int) -> None:
         """Fault injection: in the next run, range `range_index` never publishes."""
         _lib.check(self._lib.apsep_debug_inject(self._h, int(range_index), int(spin_limit)), "apsep_debug_inject")

@@ -342,6 +342,16 @@ apsep_status apsep_plan_check(apsep_plan* p, void* stream) {
     return APSEP_EINTERNAL;
 }
 
+apsep_status apsep_plan_error_async(apsep_plan* p, uint32_t* host_word, void* stream) {
+    if (!p || !host_word) return APSEP_EINVAL;
+    DeviceGuard g(p->device);
+    if (!g.ok) return APSEP_ECUDA;
+    return cudaMemcpyAsync(host_word, &p->rs.ctr->err, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           (cudaStream_t)stream) == cudaSuccess
+               ? APSEP_OK
+               : APSEP_ECUDA;
+}
+
 apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dtype dtype, apsep_cmp cmp) {
     if (n == 0) return APSEP_OK;
     apsep_plan* p = nullptr;

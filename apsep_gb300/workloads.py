@@ -6,12 +6,12 @@ uniform keys in [0, 2^31) (s % 3 == 0), strictly descending runs of length
 U[1, 4096] from random starts (s % 3 == 1), or the sawtooth k % 257
 (s % 3 == 2).  Generated on the GPU from a seeded torch generator.
 
-serve_requests: `count` requests with log-uniform lengths in [2^10, 2^24]
+pool_requests: `count` requests with log-uniform lengths in [2^10, 2^24]
 (mean about 1.7e6 keys), key type int32 / float32 50/50, Poisson arrivals at
 `rate` per second.  int32 keys are uniform in [0, 2^31); float32 keys are
 -1e6 + u * (2e6 / 2^24) with u uniform in [0, 2^24) (finite, exact).  Each
-request's keys are a slice of one pinned host pool per key type, so the
-workload needs 128 MiB of pinned memory whatever the request count.
+request owns its keys and its answer buffer: device memory (generated on the
+GPU), or pinned host memory.
 """
 from __future__ import annotations
 
@@ -60,55 +60,35 @@ def batch_workload(S: int = 4096, seed: int = 7, device="cuda") -> tuple[torch.T
     return x, offs
 
 
-def serve_requests(count: int, rate: float, seed: int = 11, lo: int = 1 << 10, hi: int = 1 << 24):
-    """Requests of the served workload (see the module docstring)."""
+def pool_requests(count: int, rate: float, seed: int = 11, lo: int = 1 << 10, hi: int = 1 << 24,
+                  device_keys: bool = True, device="cuda"):
+    """The served workload for PoolServer: lengths log-uniform in [lo, hi],
+    int32 / float32 50/50 (the value distributions above), Poisson
+    arrivals at `rate` per second.  device_keys: every request owns its keys
+    and its answer buffer in device memory (generated on the GPU); else the
+    keys are pinned host slices and the answers go to pinned host buffers."""
     from .serve import Request
 
     rng = np.random.default_rng(seed)
-    pool_i = torch.from_numpy(rng.integers(0, 1 << 31, hi, dtype=np.int64).astype(np.int32)).pin_memory()
-    u = rng.integers(0, 1 << 24, hi)
-    pool_f = torch.from_numpy((-1e6 + u * (2e6 / (1 << 24))).astype(np.float32)).pin_memory()
     lengths = segment_lengths(count, lo, hi, seed + 1)
     gaps = rng.exponential(1.0 / rate, count) if rate > 0 else np.zeros(count)
     arrivals = np.cumsum(gaps)
+    kinds = rng.random(count) < 0.5
+    g = torch.Generator(device=device if device_keys else "cpu")
+    g.manual_seed(seed)
     reqs = []
     for i in range(count):
         L = int(lengths[i])
-        start = int(rng.integers(0, hi - L + 1))
-        pool = pool_i if rng.random() < 0.5 else pool_f
-        reqs.append(Request(rid=i, keys=pool[start:start + L], arrival=float(arrivals[i])))
+        where = device if device_keys else "cpu"
+        u = torch.randint(0, 1 << 31, (L,), generator=g, device=where, dtype=torch.int64)
+        if kinds[i]:
+            keys = u.to(torch.int32)
+        else:
+            keys = (-1e6 + (u & ((1 << 24) - 1)).to(torch.float64) * (2e6 / (1 << 24))).to(torch.float32)
+        if device_keys:
+            out = torch.empty(L, dtype=torch.int32, device=device)
+        else:
+            keys = keys.pin_memory()
+            out = torch.empty(L, dtype=torch.int32).pin_memory()
+        reqs.append(Request(rid=i, keys=keys, arrival=float(arrivals[i]), out=out))
     return reqs
-
-
-def resident_requests(count: int, rate: float, seed: int = 11, lo: int = 1 << 10, hi: int = 1 << 24,
-                      dtype=torch.int32, device="cuda"):
-    """The served workload's lengths and arrivals, keys generated in place in a
-    device ring in arrival order, each request in a slot of whole 4-key units
-    (so every request starts on a 16-byte boundary; the up to 3 keys after a
-    request hold padding: INT_MAX / +inf).  Returns (keys, answers, requests)."""
-    from .serve import RESIDENT_SLOT_KEYS, ResidentRequest
-
-    rng = np.random.default_rng(seed)
-    lengths = segment_lengths(count, lo, hi, seed + 1)
-    gaps = rng.exponential(1.0 / rate, count) if rate > 0 else np.zeros(count)
-    arrivals = np.cumsum(gaps)
-    slots = (lengths + RESIDENT_SLOT_KEYS - 1) // RESIDENT_SLOT_KEYS * RESIDENT_SLOT_KEYS
-    starts = np.zeros(count, dtype=np.int64)
-    starts[1:] = np.cumsum(slots)[:-1]
-    n = int(slots.sum())
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
-    if dtype == torch.int32:
-        keys = torch.randint(0, 1 << 31, (n,), generator=g, device=device, dtype=torch.int64).to(torch.int32)
-        pad = float(2**31 - 1)
-    else:
-        u = torch.randint(0, 1 << 24, (n,), generator=g, device=device, dtype=torch.int64)
-        keys = (-1e6 + u.to(torch.float64) * (2e6 / (1 << 24))).to(torch.float32)
-        pad = float("inf")
-    fill = np.concatenate([np.arange(s + L, s + S) for s, L, S in zip(starts, lengths, slots)]).astype(np.int64)
-    if fill.size:
-        keys[torch.from_numpy(fill).to(device)] = pad
-    answers = torch.empty(n, dtype=torch.int32, device=device)
-    reqs = [ResidentRequest(rid=i, start=int(starts[i]), n=int(lengths[i]), arrival=float(arrivals[i]))
-            for i in range(count)]
-    return keys, answers, reqs

@@ -42,13 +42,16 @@ Extra objects on the same line (one GPU only; --no-extras skips them):
   batched    4096 arrays, log-uniform lengths in [32, 2^20] (4.1e8 keys), in
              one apsep_run_segmented launch vs a loop of one apsep_run per
              array on one stream; useful bytes 8*sum(L) + 8*(S+1).
-  served     the serving loop (apsep_gb300.serve): requests with log-uniform
-             lengths in [2^10, 2^24], int32 / float32 50/50, host keys in and
-             answers out through device-resident pools within an 8 GiB HBM
-             budget.  Saturated throughput against the plain per-request loop,
-             then p50/p99 latency at a Poisson offered load of half the
-             server's saturated rate.  served.resident: the same stream with
-             the keys already in a device ring (batches run in place).
+  served     the serving loop (apsep_gb300.serve.PoolServer, continuous
+             batching over device-resident pools within an 8 GiB HBM budget):
+             400 requests with log-uniform lengths in [2^10, 2^24], int32 /
+             float32 50/50, keys in device memory, answers left in the pool.
+             Saturated throughput against one apsep_run per request
+             (synchronised), p50/p99 latency at a Poisson offered load of half
+             the server's saturated rate, and 1 % of the requests checked
+             against the CPU oracle.  served.host_keys: the same stream with
+             keys and answers in pinned host memory (host-link bound; the
+             link's rates in served.host_link).
   consumers  previous greater, next smaller, stock span, Cartesian parents and
              largest rectangle at N = 2^25 (apsep_gb300.consumers): time,
              useful GB/s and the fraction of peak of all their HBM passes.
@@ -461,57 +464,97 @@ def run_long64(dev, peak_gbs: float) -> dict:
     return {"workload": "positions64_2p32_int32", "n": n, "pieces": 2, "bytes_per_key": 12, "runs": res}
 
 
-def run_served(dev) -> dict:
-    from apsep_gb300.serve import Server, plain_loop
-    from apsep_gb300.workloads import serve_requests
+SERVE_REQUESTS = 400
+SERVE_BATCH_KEYS = 1 << 27  # 128 Mi keys per launch at most
+SERVE_SAMPLE_EVERY = 100    # 1 % of the requests are checked against the CPU oracle
 
-    server = Server(budget_bytes=8 << 30, slot_keys=48 << 20, device=dev)
+
+def _served_stream(dev, device_keys: bool, rate: float, seed: int) -> dict:
+    """One stream through PoolServer against device_loop: saturated (all at
+    once) throughput of both, then p50/p99 at an offered load of half the
+    server's saturated rate, and the sampled oracle check."""
+    import oracle
+    from apsep_gb300.serve import PoolServer, Request, device_loop
+    from apsep_gb300.workloads import pool_requests
+
+    reqs = pool_requests(SERVE_REQUESTS, rate=0.0, seed=seed, device_keys=device_keys, device=dev)
+    if device_keys:  # answers stay in the pool; the sampled ones go to host memory
+        sampled = {r.rid for r in reqs if r.rid % SERVE_SAMPLE_EVERY == 0}
+        for r in reqs:
+            r.out = torch_pinned_i32(r.n) if r.rid in sampled else None
+    srv = PoolServer(budget_bytes=8 << 30, lanes_per_kind=2, max_batch_keys=SERVE_BATCH_KEYS, device=dev)
     try:
-        server.serve(serve_requests(32, rate=0.0, seed=3), realtime=False)  # warm-up
-        sat = server.serve(serve_requests(400, rate=0.0, seed=21), realtime=False)
-        base = plain_loop(serve_requests(400, rate=0.0, seed=21), realtime=False, device=dev)
-        rate = 0.5 * sat.requests_per_s
-        live = server.serve(serve_requests(400, rate=rate, seed=22), realtime=True)
-    finally:
-        server.close()
-    resident = run_served_resident(dev)
-    return {"workload": "serve_loguniform_2p10_2p24_i32_f32", "budget_bytes": 8 << 30, "resident": resident,
-            "pool_bytes": sat.device_bytes, "saturated": sat.as_dict(), "plain_loop_saturated": base.as_dict(),
-            "throughput_vs_plain_loop": round(sat.requests_per_s / base.requests_per_s, 2),
-            "offered_load_req_per_s": round(rate, 1), "at_offered_load": live.as_dict(),
-            "note": "wall clock on the host; every request copies its keys in and its answers out"}
-
-
-def run_served_resident(dev) -> dict:
-    """The same request stream with keys already in a device ring (int32)."""
-    import torch
-
-    from apsep_gb300.serve import ResidentServer, resident_loop
-    from apsep_gb300.workloads import resident_requests
-
-    keys, answers, reqs = resident_requests(400, rate=0.0, seed=23, device=dev)
-    srv = ResidentServer(keys, answers, max_batch_keys=160 << 20)
-    try:
-        srv.serve(reqs[:32], realtime=False)  # warm-up
-        sat = srv.serve(reqs, realtime=False)
-        base = resident_loop(keys, answers, reqs, realtime=False)
-        rate = 0.5 * sat.requests_per_s
-        keys2, answers2, reqs2 = resident_requests(400, rate=rate, seed=24, device=dev)
-        srv2 = ResidentServer(keys2, answers2, max_batch_keys=160 << 20)
-        try:
-            live = srv2.serve(reqs2, realtime=True)
-        finally:
-            srv2.close()
+        srv.serve(reqs[:40], realtime=False)  # warm-up
+        sat = max((srv.serve(reqs, realtime=False) for _ in range(3)), key=lambda st: st.requests_per_s)
+        # the sampled requests' answers (the last saturated pass) against the oracle
+        ok = True
+        for r in reqs:
+            if r.rid % SERVE_SAMPLE_EVERY == 0:
+                k = r.keys.cpu().numpy() if r.keys.is_cuda else r.keys.numpy()
+                ok = ok and not r.failed and bool((r.out[:r.n].cpu().numpy() == oracle.apse(k)).all())
+        base = max((device_loop(reqs, realtime=False, device=dev) for _ in range(2)),
+                   key=lambda st: st.requests_per_s)
+        # the same requests arriving as a Poisson stream at half the saturated rate
+        live_rate = 0.5 * sat.requests_per_s
+        gaps = np.random.default_rng(seed + 1).exponential(1.0 / live_rate, len(reqs))
+        live_reqs = [Request(rid=r.rid, keys=r.keys, arrival=float(t), out=None if device_keys else r.out)
+                     for r, t in zip(reqs, np.cumsum(gaps))]
+        live = srv.serve(live_reqs, realtime=True)
+        failed = sum(r.failed for r in reqs) + sum(r.failed for r in live_reqs)
     finally:
         srv.close()
-    del keys, answers
-    torch.cuda.empty_cache()
-    return {"workload": "serve_resident_loguniform_2p10_2p24_i32", "budget_bytes": 8 << 30,
-            "pool_bytes": sat.device_bytes,
+    return {"keys_in": "device" if device_keys else "pinned host", "pool_bytes": srv.device_bytes,
             "saturated": sat.as_dict(), "plain_loop_saturated": base.as_dict(),
             "throughput_vs_plain_loop": round(sat.requests_per_s / base.requests_per_s, 2),
-            "offered_load_req_per_s": round(rate, 1), "at_offered_load": live.as_dict(),
-            "note": "keys produced in place in a device ring; batches run in place, no copies"}
+            "offered_load_req_per_s": round(live_rate, 1), "at_offered_load": live.as_dict(),
+            "sampled_requests": len(range(0, SERVE_REQUESTS, SERVE_SAMPLE_EVERY)), "sampled_bit_exact": ok,
+            "failed_requests": int(failed)}
+
+
+def torch_pinned_i32(n: int):
+    import torch
+    return torch.empty(n, dtype=torch.int32).pin_memory()
+
+
+def host_link_gbs(dev) -> dict:
+    """Pinned host <-> device copy rates of this machine (256 MiB each way)."""
+    import torch
+    h = torch.empty(1 << 26, dtype=torch.int32).pin_memory()
+    d = torch.empty(1 << 26, dtype=torch.int32, device=dev)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    best = [0.0, 0.0]
+    for _ in range(3):
+        e[0].record()
+        d.copy_(h, non_blocking=True)
+        e[1].record()
+        h.copy_(d, non_blocking=True)
+        e[2].record()
+        torch.cuda.synchronize(dev)
+        best[0] = max(best[0], 2**28 / e[0].elapsed_time(e[1]) / 1e6)
+        best[1] = max(best[1], 2**28 / e[1].elapsed_time(e[2]) / 1e6)
+    return {"h2d_gbs": round(best[0], 1), "d2h_gbs": round(best[1], 1)}
+
+
+def run_served(dev) -> dict:
+    """The served request stream (PoolServer, continuous batching): 400
+    requests, lengths log-uniform in [2^10, 2^24], int32 / float32 50/50, an
+    8 GiB pool budget; keys and answers in device memory (the headline), and
+    the same stream with keys and answers in pinned host memory (bound by the
+    host link, whose rates are reported beside it)."""
+    import torch
+
+    dev_stream = _served_stream(dev, device_keys=True, rate=0.0, seed=21)
+    torch.cuda.empty_cache()
+    host_stream = _served_stream(dev, device_keys=False, rate=0.0, seed=41)
+    torch.cuda.empty_cache()
+    out = {"workload": "serve_loguniform_2p10_2p24_i32_f32", "budget_bytes": 8 << 30, "requests": SERVE_REQUESTS,
+           "max_batch_keys": SERVE_BATCH_KEYS}
+    out.update(dev_stream)
+    out["host_keys"] = host_stream
+    out["host_link"] = host_link_gbs(dev)
+    out["note"] = ("wall clock on the host; throughput_vs_plain_loop: the same requests through one apsep_run each "
+                   "(device_loop), synchronised after each")
+    return out
 
 
 def pipelined_e2e_ms(plan, pinned_in: dict, n: int, steps: int, dev) -> float:
@@ -761,19 +804,13 @@ def run_ours(args) -> None:
         plan.close()
         del d_in, out, flush
         torch.cuda.empty_cache()
-        line["batched"] = run_batched(dev)
-        torch.cuda.empty_cache()
-        line["served"] = run_served(dev)
-        torch.cuda.empty_cache()
-        line["consumers"] = run_consumers(dev, peaks["hbm_gbs"])
-        torch.cuda.empty_cache()
-        line["wide"] = run_wide(dev, peaks["hbm_gbs"])
-        torch.cuda.empty_cache()
-        line["long64"] = run_long64(dev, peaks["hbm_gbs"])
-        torch.cuda.empty_cache()
-        line["le"] = run_le(dev, peaks["hbm_gbs"])
-        torch.cuda.empty_cache()
-        line["sweep"] = run_sweep(dev, peaks["hbm_gbs"])
+        legs = {"batched": lambda: run_batched(dev), "served": lambda: run_served(dev),
+                "consumers": lambda: run_consumers(dev, peaks["hbm_gbs"]),
+                "wide": lambda: run_wide(dev, peaks["hbm_gbs"]), "long64": lambda: run_long64(dev, peaks["hbm_gbs"]),
+                "le": lambda: run_le(dev, peaks["hbm_gbs"]), "sweep": lambda: run_sweep(dev, peaks["hbm_gbs"])}
+        for name in (args.extras.split(",") if args.extras else legs):
+            line[name] = legs[name]()
+            torch.cuda.empty_cache()
     print(json.dumps(line), flush=True)
     if world > 1 or args.no_extras:
         plan.close()
@@ -789,6 +826,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / served / sweep objects")
+    ap.add_argument("--extras", default="", help="comma-separated subset of the extra objects (default: all)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

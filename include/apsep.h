@@ -119,6 +119,15 @@ apsep_status apsep_run_segmented(apsep_plan* plan, const void* d_in, int32_t* d_
  * offsets), clearing them. */
 apsep_status apsep_plan_check(apsep_plan* plan, void* stream);
 
+/* Enqueue on `stream` a copy of the plan's sticky device-side error word into
+ * *host_word (pinned host memory; nonzero = some earlier run on this plan hit
+ * an error), without synchronising.  A caller that keeps many runs in flight
+ * reads the word once the stream has passed the copy, and calls
+ * apsep_plan_check (which decodes and clears the error) only when it is
+ * nonzero, so a failure is tied to the runs before that copy.  No counterpart
+ * in the reference (its gpuAssert exits the process). */
+apsep_status apsep_plan_error_async(apsep_plan* plan, uint32_t* host_word, void* stream);
+
 /* Plan facts (capacity, scratch bytes, tile size, configuration). */
 apsep_status apsep_plan_get_info(const apsep_plan* plan, apsep_plan_info* info);
 
@@ -222,6 +231,15 @@ apsep_status apsep_cartesian_parents(apsep_plan* plan, const void* d_in, int32_t
 int64_t apsep_run64_workspace_bytes(const apsep_plan* plan, int64_t n);
 apsep_status apsep_run64(apsep_plan* plan, const void* d_in, int64_t* d_out, int64_t n, apsep_cmp cmp,
                          void* d_work, void* stream);
+
+/* Copy nspans byte spans, src[i] -> dst[i] (bytes[i] bytes each; device
+ * memory, or host memory the device can address; spans must not overlap),
+ * in one kernel launch per 256 spans, asynchronously on `stream`.  The
+ * serving layer's gather of admitted requests' keys into its device pool
+ * and scatter of their answers: one call instead of one memcpy per request.
+ * No counterpart in the reference (it has no serving layer). */
+apsep_status apsep_copy_spans(const void* const* src, void* const* dst, const int64_t* bytes, int32_t nspans,
+                              void* stream);
 
 /* Fault injection for failure-detection tests: in the next run, range `range`
  * (the contiguous block of tiles one persistent warp sweeps) never publishes

@@ -65,6 +65,9 @@ def test_argument_validation_without_device(built_lib):
     assert lib.apsep_run(None, None, None, 5, None) == _lib.APSEP_EINVAL
     assert lib.apsep_plan_destroy(None) == _lib.APSEP_OK
     assert lib.apsep_plan_check(None, None) == _lib.APSEP_EINVAL
+    assert lib.apsep_plan_error_async(None, None, None) == _lib.APSEP_EINVAL
+    assert lib.apsep_copy_spans(None, None, None, -1, None) == _lib.APSEP_EINVAL
+    assert lib.apsep_copy_spans(None, None, None, 3, None) == _lib.APSEP_EINVAL
     assert lib.apsep_plan_set_config(None, 0) == _lib.APSEP_EINVAL
     assert lib.apsep_debug_inject(None, -2, 0) == _lib.APSEP_EINVAL
     assert lib.apsep_debug_inject(None, -1, 0) == _lib.APSEP_OK  # (no plan: the no-alloc path, disarmed)

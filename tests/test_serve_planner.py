@@ -1,40 +1,10 @@
-"""Host logic of the serving loop (no GPU): FIFO admission by slot capacity
-and segment count, and the latency statistics."""
-import collections
-
+"""Host logic of the serving loop (no GPU): the ring allocator of the pools
+(spans, wrap-around, reclamation from the tail) and the latency statistics."""
 import pytest
 
 torch = pytest.importorskip("torch")
 
-from apsep_gb300.serve import BatchPlanner, Request, ServeStats  # noqa: E402
-
-
-def req(i, n):
-    return Request(rid=i, keys=torch.empty(n, dtype=torch.int32))
-
-
-def test_takes_longest_fitting_prefix_in_arrival_order():
-    p = BatchPlanner(capacity_keys=100, max_segments=10)
-    q = collections.deque([req(0, 40), req(1, 50), req(2, 20), req(3, 5)])
-    b = p.take(q)
-    assert [r.rid for r in b] == [0, 1]          # 90 keys; request 2 would overflow
-    assert [r.rid for r in q] == [2, 3]          # FIFO order kept, no overtaking
-    assert [r.rid for r in p.take(q)] == [2, 3]
-
-
-def test_segment_limit_and_empty_requests():
-    p = BatchPlanner(capacity_keys=1000, max_segments=3)
-    q = collections.deque([req(i, 0 if i % 2 else 7) for i in range(7)])
-    assert [r.rid for r in p.take(q)] == [0, 1, 2]
-    assert len(q) == 4
-
-
-def test_oversized_request_is_not_admissible():
-    p = BatchPlanner(capacity_keys=64, max_segments=8)
-    assert p.fits(64) and not p.fits(65)
-    q = collections.deque([req(0, 65), req(1, 1)])
-    assert p.take(q) == []                       # the head does not fit: nothing overtakes it
-    assert len(q) == 2
+from apsep_gb300.serve import ServeStats  # noqa: E402
 
 
 def test_stats():
@@ -45,3 +15,52 @@ def test_stats():
     assert s.p99_ms > 90.0
     d = s.as_dict()
     assert d["useful_gbs"] == round(8 * 200 / 1e9, 2) and d["batches"] == 2
+
+
+def test_ring_pool_allocates_wraps_and_reclaims():
+    from apsep_gb300.serve import RingPool
+    p = RingPool(100, align=4)
+    assert p.capacity == 100
+    a = p.alloc(30)   # 32 slots
+    b = p.alloc(50)   # 52
+    assert (a, b) == (0, 32)
+    assert p.alloc(20) is None          # 84 + 20 > 100 and nothing free at the tail yet
+    c = p.alloc(13)                     # 16 -> 84..100
+    assert c == 84 and p.used == 100
+    assert p.alloc(1) is None           # full
+    p.free(b)                           # out of order: the tail stays at 0
+    assert p.used == 100 and p.alloc(4) is None
+    p.free(a)                           # tail reclaimed up to c
+    assert p.used == 16
+    d = p.alloc(60)                     # wraps to the start
+    assert d == 0
+    assert p.alloc(30) is None          # only 84 - 60 = 24 free before the tail
+    e = p.alloc(24)
+    assert e == 60 and p.used == 100
+    p.free(c)
+    p.free(d)
+    p.free(e)
+    assert p.used == 0 and p.alloc(100) == 0
+
+
+def test_ring_pool_spans_are_aligned_and_never_overlap():
+    import random
+    from apsep_gb300.serve import RingPool
+    rnd = random.Random(5)
+    p = RingPool(1000, align=4)
+    live = {}
+    for _ in range(5000):
+        if live and (rnd.random() < 0.45 or len(live) > 20):
+            s = rnd.choice(list(live))
+            p.free(s)
+            del live[s]
+        else:
+            n = rnd.randint(0, 300)
+            s = p.alloc(n)
+            if s is not None:
+                size = p.span_size(n)
+                assert s % 4 == 0 and s + size <= 1000
+                for t, z in live.items():
+                    assert s + size <= t or t + z <= s
+                live[s] = size
+    assert p.alloc(2000) is None
