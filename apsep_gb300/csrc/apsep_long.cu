@@ -337,6 +337,19 @@ apsep_status apsep_run64(apsep_plan* plan, const void* d_in, int64_t* d_out, int
         return APSEP_EINVAL;
     const int64_t piece = piece_keys(info.capacity, n);
     const cudaStream_t st = (cudaStream_t)stream;
+    // the whole call on the plan's device (the engine runs there; so must the
+    // widening and level passes, sized from that device's SMs), the caller's
+    // device restored afterwards
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return APSEP_ECUDA;
+    if (prev != info.device && cudaSetDevice(info.device) != cudaSuccess) return APSEP_ECUDA;
+    struct Restore {
+        int dev;
+        ~Restore() {
+            int cur = -1;
+            if (cudaGetDevice(&cur) == cudaSuccess && cur != dev) cudaSetDevice(dev);
+        }
+    } restore{prev};
     switch (info.dtype) {
     case APSEP_INT32: return run_long<int32_t, false>(plan, (const int32_t*)d_in, d_out, n, cmp, piece, d_work, st);
     case APSEP_FLOAT32: return run_long<float, false>(plan, (const float*)d_in, d_out, n, cmp, piece, d_work, st);

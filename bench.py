@@ -16,8 +16,10 @@ beside it.
              read, so no line of the inputs stays cached and no dirty line of
              the flush is left for the timed kernel to write back.
   per_distribution  median (with p10 / p90) device time per distribution,
-             and the median of the same steps back to back without the
-             flush.
+             the median of the same steps back to back without the flush, and
+             the steady state (us_steady, frac_steady): 20 runs of one
+             distribution back to back between one pair of events, as the
+             reference times its kernels.
   reference_published  the reference's published SPT figures at N = 2^25
              (one GTX 1660 Ti, per distribution) and ours over them:
              context only, other hardware.
@@ -28,7 +30,8 @@ beside it.
              device buffers each way; whole-loop time); serial: one step at a
              time on one stream, events around each step.
   roofline   achieved = algorithmic bytes per launch (8 B/key) / mean launch
-             time, against the measured HBM copy bandwidth
+             time (roofline.steady_state: the same from the steady-state
+             times), against the measured HBM copy bandwidth
              (MEASURED_PEAKS.json); traffic = DRAM bytes per launch from the
              committed ncu summary (profiles/), when present.
   cpu_baseline  the sequential monotone-stack oracle on one host core over a
@@ -91,6 +94,7 @@ DISTS = ("uniform", "descending", "ascending", "dup16")
 METRIC = "useful GB/s at N=32M (frac. of HBM peak)"
 UNIT = "GB/s"
 WORKLOAD = "apse_single_2p25_int32"
+STEADY_RUNS = 20
 
 
 def make_inputs(n: int = N, seed: int = 20250325) -> dict[str, np.ndarray]:
@@ -721,6 +725,19 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
     plan.check()
     step_ms_unflushed = [a.elapsed_time(b) for a, b in ev_u]
+    # steady state, as the reference times (src/main.cu:125-142): STEADY_RUNS runs of
+    # one distribution back to back between one pair of events, no flush
+    steady_ms = {}
+    for name in DISTS:
+        plan.run(d_in[name], out=out)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(STEADY_RUNS):
+            plan.run(d_in[name], out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        steady_ms[name] = e0.elapsed_time(e1) / STEADY_RUNS
+    plan.check()
 
     # e2e through the public API: pinned host -> device, run, device -> host.
     # (a) serial: one step at a time on one stream (L2 flushed before each);
@@ -762,13 +779,17 @@ def run_ours(args) -> None:
             per[name] = {"gbs": round(useful_gbs(N, statistics.median(ms) / 1e3), 1),
                          "us_median": round(statistics.median(ms) * 1e3, 2),
                          "us_p10": round(pct(ms, 0.1) * 1e3, 2), "us_p90": round(pct(ms, 0.9) * 1e3, 2),
-                         "us_median_unflushed": round(statistics.median(mu) * 1e3, 2)}
+                         "us_median_unflushed": round(statistics.median(mu) * 1e3, 2),
+                         "us_steady": round(steady_ms[name] * 1e3, 2)}
     peaks = measured_peaks()
     mean_s = total_ms / 1e3 / args.steps
     achieved = 8.0 * N / mean_s / 1e9
     traffic = profile_traffic()
     for name in per:
         per[name]["frac"] = round(per[name]["gbs"] / peaks["hbm_gbs"], 4)
+        per[name]["frac_steady"] = round(useful_gbs(N, per[name]["us_steady"] / 1e6) / peaks["hbm_gbs"], 4)
+    steady_mean_s = sum(steady_ms.values()) / len(steady_ms) / 1e3
+    steady_achieved = 8.0 * N / steady_mean_s / 1e9
     # The reference's only published numbers for this metric: SPT at N = 2^25 on one
     # GTX 1660 Ti (README.md:27-29), per distribution; other hardware, so context
     # only (vs_baseline stays null: no published figure for this aggregate on GB300).
@@ -790,7 +811,11 @@ def run_ours(args) -> None:
                      "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_launch": 8 * N,
                      "traffic": traffic.get("bytes_per_launch") if traffic else None,
-                     "traffic_source": traffic.get("source") if traffic else None},
+                     "traffic_source": traffic.get("source") if traffic else None,
+                     "steady_state": {"achieved": round(steady_achieved, 1),
+                                      "frac": round(steady_achieved / peaks["hbm_gbs"], 4),
+                                      "how": "%d runs of each distribution back to back between one pair of "
+                                             "CUDA events, no L2 flush; mean over the four" % STEADY_RUNS}},
         "e2e": {"value": round(whole_job_gbs(N, e2e_ms, args.steps, world), 2), "unit": UNIT,
                 "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N, "form": "pipelined",
                 "serial": round(whole_job_gbs(N, e2e_serial_ms, args.steps, world), 2)},

@@ -10,10 +10,10 @@ oracle/_ref/apsep_ref_spt.ptx (compute_103a; loaded by the GPU tests through
 the driver API, so it needs no host code of this machine's architecture).
 Nothing is copied out of the reference; both outputs are git-ignored.
 
-The reference tree is looked up in $APSEP_REFERENCE_DIR, else at
-/root/reference.  When it is absent (e.g. on a machine that only has this
-repository) build() returns None and the callers fall back to the oracle
-restatement, saying so.
+The reference tree is looked up in $APSEP_REFERENCE_DIR, else in a directory
+named `reference` beside this repository's root.  When it is absent (e.g. on
+a machine that only has this repository) build() returns None and the callers
+fall back to the oracle restatement, saying so.
 
 Flags: -std=c++17 (the reference Makefile's -std=c++14 no longer compiles
 against CUDA 13's cooperative-groups headers), and -DmemoryClockRate=... to
@@ -34,8 +34,11 @@ LIB = os.path.join(OUT_DIR, "libapsep_ref_cpu.so")
 SPT_PTX = os.path.join(OUT_DIR, "apsep_ref_spt.ptx")
 
 
+REPO_ROOT = os.path.dirname(HERE)
+
+
 def reference_dir() -> str | None:
-    d = os.environ.get("APSEP_REFERENCE_DIR", "/root/reference")
+    d = os.environ.get("APSEP_REFERENCE_DIR") or os.path.join(os.path.dirname(REPO_ROOT), "reference")
     src = os.path.join(d, "src")
     if os.path.isfile(os.path.join(src, "main.cu")) and os.path.isfile(
             os.path.join(src, "bench_spt_le.cu")):

@@ -270,3 +270,20 @@ def test_graph_capture_of_pieces(plans):
         torch.cuda.synchronize()
         assert np.array_equal(out.cpu().numpy(), oracle.apse(a).astype(np.int64)), name
     plan.check()
+
+
+def test_run64_while_another_device_is_current():
+    """apsep_run64 runs on its plan's device whatever device is current, and
+    leaves the caller's device current."""
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    n = 3 * 4096 + 5
+    a = np.random.default_rng(12).integers(0, 1 << 31, n, dtype=np.int64).astype(np.int32)
+    with torch.cuda.device(1):
+        with Plan(4096, torch.int32, device=1) as plan:
+            x = torch.from_numpy(a).to("cuda:1")
+            torch.cuda.set_device(0)
+            out = plan.run64(x)
+            assert torch.cuda.current_device() == 0
+            plan.check()
+            assert np.array_equal(out.cpu().numpy(), oracle.apse(a).astype(np.int64))
