@@ -585,6 +585,86 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             const int lb = tile_base + lane * IPT;  // position of this lane's first key
             const int nvalid = min(max(a.n - lb, 0), IPT);
+            // Flagged keys, deferred (dm) and capped (cm), keep -1 in O.  The first kDefCap
+            // deferred and kCapCap capped keys of the range go to in-order lists in shared
+            // memory for phase 2; every tile also leaves its flags in global memory for the
+            // lists' overflow.
+            auto flag_keys = [&](const unsigned dm, const unsigned cm) {
+                {
+                    const unsigned fm = dm | cm;
+                    const int nd = __popc(dm), nc = __popc(cm);
+                    const unsigned anyf = __ballot_sync(FULL, fm != 0);
+                    int dtot = 0, ctot = 0;
+                    if (anyf) {
+                        const int doff = warp_excl_sum(nd, dtot);
+                        const int coff = warp_excl_sum(nc, ctot);
+                        {
+                            int idx = def_total + doff;
+                            unsigned m = dm;
+                            while (m && idx < kDefCap) {
+                                const int k = __ffs(m) - 1;
+                                m &= m - 1;
+                                sDefP[idx] = lb + k;
+                                sDefV[idx] = V[ks(lane * IPT + k)];
+                                idx++;
+                            }
+                        }
+                        {
+                            int idx = cap_total + coff;
+                            unsigned m = cm;
+                            while (m && idx < kCapCap) {
+                                const int k = __ffs(m) - 1;
+                                m &= m - 1;
+                                if constexpr (SEG) sCapS[idx] = seg_of(k);
+                                sCapP[idx++] = lb + k;
+                            }
+                        }
+                        // mask word w covers keys [32w, 32w + 32): lanes TPC*w .. TPC*w + TPC - 1
+                        uint32_t mw = 0;
+    #pragma unroll
+                        for (int j = 0; j < TPC; j++) {
+                            const unsigned part = __shfl_sync(FULL, fm, (lane % W) * TPC + j);
+                            mw |= part << (j * IPT);
+                        }
+                        if (lane < W) __stcg(&a.s.tile_mask[(size_t)t * MW + lane], mw);
+                        def_total += dtot;
+                        cap_total += ctot;
+                    }
+                    if (lane == 0) __stcg(&a.s.tile_flag[t], (uint32_t)(dtot + ctot) | (ctot ? 0x80000000u : 0u));
+                }
+            };
+            // The whole tile leaves O, flagged keys as -1 (segmented runs: answers made
+            // relative to their segment's start).
+            auto store_tile = [&]() {
+                if constexpr (SEG) {  // answers relative to their segment's start
+                    __syncwarp();     // every lane's answers are in O
+    #pragma unroll
+                    for (int q4 = 0; q4 < IPT / 4; q4++) {
+                        int4* po = reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]);
+                        int4 o = *po;
+                        o.x = seg_rel(o.x, seg_of(4 * q4 + 0));
+                        o.y = seg_rel(o.y, seg_of(4 * q4 + 1));
+                        o.z = seg_rel(o.z, seg_of(4 * q4 + 2));
+                        o.w = seg_rel(o.w, seg_of(4 * q4 + 3));
+                        *po = o;
+                    }
+                }
+                fence_proxy_async_smem();
+                __syncwarp();
+                if (full) {
+                    if (lane == 0) {
+                        tma_store_2d(&map_out, 0, t * W, O);
+                        bulk_commit();
+                    }
+                } else {
+    #pragma unroll
+                    for (int j = 0; j < IPT; j++) {
+                        const int e = j * 32 + lane;
+                        if (e < valid_keys && (!head || tile_base + e >= head)) a.d_out[tile_base + e] = O[swz(e)];
+                    }
+                }
+            };
+
             // Monotone lanes: each key answers its neighbour (adj), or no key answers
             // any later one (none); across the lane boundary likewise (b_adj, b_none).
             // A few neighbour pairs first: on almost every tile of unordered keys some
@@ -736,6 +816,74 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 }
             }
 
+            // Filled by the path below that handles the tile (steps 1-5, or a tile that never
+            // increases) and used by steps 6-9.
+            unsigned dm = 0u, cm = 0u;
+            T lmin = KeyTraits<T>::pad(), suf = KeyTraits<T>::pad(), tile_min_t = KeyTraits<T>::pad();
+            T wv = KeyTraits<T>::pad();
+            int win_lo = 0, dkeep = 0;
+            bool wvalid = false;
+            // ---- a whole tile that never increases, above something earlier in the range -----
+            // No key answers another, so every key's answer is the topmost qualifying entry
+            // of the range stack (else it is capped or deferred), and as the keys do not
+            // increase those entries only move down the stack: each lane searches the
+            // stack for its first key, then walks down for the others.  The stack keeps
+            // its entries below the tile's last key and takes that key.  Segmented
+            // instantiations only (descending runs in batches of segments are made of
+            // such tiles): in the single-array kernel the extra branch cost 5 us on
+            // random keys at 2^25.
+            const bool dtile =
+                SEG && mono == FULL && valid_keys == WT && __all_sync(FULL, none && (lane == 0 || !b_adj));
+            if (dtile) {
+                const int dwin = max(stk_lo, stk_hi - 32);
+                const int wcnt = stk_hi - dwin;
+                const T dwv = dwin + lane < stk_hi ? sStkV[(dwin + lane) & (K - 1)] : KeyTraits<T>::pad();
+                int lo = -1;  // topmost qualifying window entry for the lane's first key
+#pragma unroll
+                for (int s2 = 32; s2 > 0; s2 >>= 1) {
+                    const int cand = lo + s2;
+                    const T wc = __shfl_sync(FULL, dwv, cand & 31);
+                    if (cand < wcnt && lt<INCL>(wc, v[0])) lo = cand;
+                }
+                int si = lo >= 0 ? dwin + lo : stk_lo - 1;  // stack index of the current answer
+                if (lo < 0 && dwin > stk_lo) {  // below the window (values increase upwards)
+                    int l2 = stk_lo, h2 = dwin;
+                    while (l2 < h2) {
+                        const int mid = (l2 + h2) >> 1;
+                        if (lt<INCL>(sStkV[mid & (K - 1)], v[0])) l2 = mid + 1;
+                        else h2 = mid;
+                    }
+                    si = l2 - 1;
+                }
+                int res[IPT];
+#pragma unroll
+                for (int k = 0; k < IPT; k++) {
+                    if (k > 0)
+                        while (si >= stk_lo && !lt<INCL>(sStkV[si & (K - 1)], v[k])) si--;
+                    if (si >= stk_lo) {
+                        res[k] = sStkP[si & (K - 1)];
+                    } else {
+                        res[k] = -1;
+                        if (has_rmin && lt<INCL>(rmin, v[k])) cm |= 1u << k;  // below the kept entries
+                        else dm |= 1u << k;
+                    }
+                }
+                if constexpr (SEG) {  // deferred keys outside the range's first segment are final (-1)
+                    if (lb + IPT > first_end) dm &= lb >= first_end ? 0u : ((1u << (first_end - lb)) - 1u);
+                }
+                if (cm && !dropped) atomicOr(err, ERR_INTERNAL);
+#pragma unroll
+                for (int q4 = 0; q4 < IPT / 4; q4++)
+                    *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) =
+                        make_int4(res[4 * q4], res[4 * q4 + 1], res[4 * q4 + 2], res[4 * q4 + 3]);
+                if (((lane + 1) & (TPC - 1)) == 0) __stcg(&chunk_min_w[(size_t)t * W + lane / TPC], v[IPT - 1]);
+                tile_min_t = __shfl_sync(FULL, v[IPT - 1], 31);
+                // the stack keeps its entries below the tile minimum (values >= it go; the
+                // search's entry may equal it under <=) and takes the tile minimum
+                int kp = __shfl_sync(FULL, si, 31);
+                while (kp >= stk_lo && !(sStkV[kp & (K - 1)] < tile_min_t)) kp--;
+                dkeep = kp + 1;
+            } else {
             unsigned umask = 0;     // keys without an in-thread answer
             bool all_inc = false;   // the whole tile increases: every key answers its predecessor
             {
@@ -770,7 +918,6 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     *reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]) =
                         make_int4(res[4 * q4], res[4 * q4 + 1], res[4 * q4 + 2], res[4 * q4 + 3]);
             }
-            T lmin;
             {  // suffix minima of the lane's keys (for the key search of X keys)
                 T sfx[IPT];
                 sfx[IPT - 1] = v[IPT - 1];
@@ -799,7 +946,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
 
             // ---- 2. warp prefix minima over lane minima ---------------------------------
-            T pre = lmin, suf = lmin;  // inclusive prefix / suffix minima over lanes, side by side
+            T pre = lmin;  // inclusive prefix / suffix minima over lanes, side by side
+            suf = lmin;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const T nb = __shfl_up_sync(FULL, pre, o);
@@ -808,7 +956,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 if (lane + o < 32) suf = KeyTraits<T>::vmin(suf, na);
             }
             const T before = __shfl_up_sync(FULL, pre, 1);  // min of the lanes before (lane > 0)
-            const T tile_min_t = __shfl_sync(FULL, pre, 31);
+            tile_min_t = __shfl_sync(FULL, pre, 31);
 
             // ---- 3. classify the keys without an in-thread answer ------------------------
             // X: answered by an earlier lane of the tile; S: by an earlier tile of the
@@ -826,7 +974,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             const unsigned xm = lane > 0 ? (umask & gtb) : 0u;
             const unsigned sm = has_rmin ? (umask & ~xm & gtr) : 0u;
-            unsigned dm = umask & ~xm & ~sm;
+            dm = umask & ~xm & ~sm;
             if constexpr (SEG) {
                 // Nothing in the range qualifies for a deferred key; if its segment
                 // starts inside the range, -1 is its final answer.  Only keys of the
@@ -941,11 +1089,11 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             // ballot.  With nothing ever dropped the bottom entry is the range minimum,
             // which qualifies; otherwise a miss is "capped": the answer lies in the
             // range below the kept entries and phase 2 finds it.
-            const int win_lo = max(stk_lo, stk_hi - 32);
+            win_lo = max(stk_lo, stk_hi - 32);
             const int widx = win_lo + lane;
-            const bool wvalid = widx < stk_hi;
-            const T wv = wvalid ? sStkV[widx & (K - 1)] : KeyTraits<T>::pad();
-            unsigned cm = 0;
+            wvalid = widx < stk_hi;
+            wv = wvalid ? sStkV[widx & (K - 1)] : KeyTraits<T>::pad();
+            cm = 0;
             if (__any_sync(FULL, sm != 0)) {
                 const int wcnt = stk_hi - win_lo;  // window entries (uniform)
                 const int wp = wvalid ? sStkP[widx & (K - 1)] : -1;
@@ -1024,85 +1172,27 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 }
                 if (cm && !dropped) atomicOr(err, ERR_INTERNAL);
             }
+            }  // steps 1-5
 
             // ---- 6. flagged keys: deferred (D) and capped (C) -----------------------------
-            // They keep -1 in O.  The first kDefCap deferred and kCapCap capped keys of
-            // the range go to in-order lists in shared memory for phase 2; every tile also
-            // leaves its flags in global memory for the lists' overflow.
-            {
-                const unsigned fm = dm | cm;
-                const int nd = __popc(dm), nc = __popc(cm);
-                const unsigned anyf = __ballot_sync(FULL, fm != 0);
-                int dtot = 0, ctot = 0;
-                if (anyf) {
-                    const int doff = warp_excl_sum(nd, dtot);
-                    const int coff = warp_excl_sum(nc, ctot);
-                    {
-                        int idx = def_total + doff;
-                        unsigned m = dm;
-                        while (m && idx < kDefCap) {
-                            const int k = __ffs(m) - 1;
-                            m &= m - 1;
-                            sDefP[idx] = lb + k;
-                            sDefV[idx] = V[ks(lane * IPT + k)];
-                            idx++;
-                        }
-                    }
-                    {
-                        int idx = cap_total + coff;
-                        unsigned m = cm;
-                        while (m && idx < kCapCap) {
-                            const int k = __ffs(m) - 1;
-                            m &= m - 1;
-                            if constexpr (SEG) sCapS[idx] = seg_of(k);
-                            sCapP[idx++] = lb + k;
-                        }
-                    }
-                    // mask word w covers keys [32w, 32w + 32): lanes TPC*w .. TPC*w + TPC - 1
-                    uint32_t mw = 0;
-#pragma unroll
-                    for (int j = 0; j < TPC; j++) {
-                        const unsigned part = __shfl_sync(FULL, fm, (lane % W) * TPC + j);
-                        mw |= part << (j * IPT);
-                    }
-                    if (lane < W) __stcg(&a.s.tile_mask[(size_t)t * MW + lane], mw);
-                    def_total += dtot;
-                    cap_total += ctot;
-                }
-                if (lane == 0) __stcg(&a.s.tile_flag[t], (uint32_t)(dtot + ctot) | (ctot ? 0x80000000u : 0u));
-            }
+            flag_keys(dm, cm);
 
             // ---- 7. output: the whole tile, flagged keys as -1 ----------------------------
-            if constexpr (SEG) {  // answers relative to their segment's start
-                __syncwarp();     // every lane's answers are in O
-#pragma unroll
-                for (int q4 = 0; q4 < IPT / 4; q4++) {
-                    int4* po = reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]);
-                    int4 o = *po;
-                    o.x = seg_rel(o.x, seg_of(4 * q4 + 0));
-                    o.y = seg_rel(o.y, seg_of(4 * q4 + 1));
-                    o.z = seg_rel(o.z, seg_of(4 * q4 + 2));
-                    o.w = seg_rel(o.w, seg_of(4 * q4 + 3));
-                    *po = o;
-                }
-            }
-            fence_proxy_async_smem();
-            __syncwarp();
-            if (full) {
-                if (lane == 0) {
-                    tma_store_2d(&map_out, 0, t * W, O);
-                    bulk_commit();
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < IPT; j++) {
-                    const int e = j * 32 + lane;
-                    if (e < valid_keys && (!head || tile_base + e >= head)) a.d_out[tile_base + e] = O[swz(e)];
-                }
-            }
+            store_tile();
 
             // ---- 8. stack update: pop what the tile dominates, push its suffix minima ----
-            {
+            if (dtile) {  // (the tile that never increases) push its minimum
+                __syncwarp();  // every lane has read the stack
+                if (lane == 31) {
+                    sStkV[dkeep & (K - 1)] = v[IPT - 1];
+                    sStkP[dkeep & (K - 1)] = tile_base + WT - 1;
+                }
+                stk_hi = dkeep + 1;
+                if (stk_hi - K > stk_lo) {
+                    stk_lo = stk_hi - K;
+                    dropped = true;
+                }
+            } else {
                 const T after_w = __shfl_down_sync(FULL, suf, 1);  // min of the lanes after (lane < 31)
                 unsigned fmask = 0;
                 const bool has_aft = lane < 31;
