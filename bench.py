@@ -44,7 +44,8 @@ is all ranks' useful bytes over the slowest rank's time.
 Extra objects on the same line (one GPU only; --no-extras skips them):
   batched    4096 arrays, log-uniform lengths in [32, 2^20] (4.1e8 keys), in
              one apsep_run_segmented launch vs a loop of one apsep_run per
-             array on one stream; useful bytes 8*sum(L) + 8*(S+1).
+             array on one stream, both replayed from CUDA graphs; useful
+             bytes 8*sum(L) + 8*(S+1).
   served     the serving loop (apsep_gb300.serve.PoolServer, continuous
              batching over device-resident pools within an 8 GiB HBM budget):
              400 requests with log-uniform lengths in [2^10, 2^24], int32 /
@@ -259,6 +260,10 @@ def run_reference(args) -> None:
 
 
 def run_batched(dev) -> dict:
+    """The batch of 4096 arrays in one segmented launch against a loop of one
+    apsep_run per array.  Both are captured in CUDA graphs and timed by
+    replaying them (device time, no host enqueue cost in either); the loop as
+    enqueued from Python is reported beside them."""
     import torch
 
     from apsep_gb300 import Plan
@@ -271,36 +276,50 @@ def run_batched(dev) -> dict:
     out = torch.empty(n, dtype=torch.int32, device=dev)
     plan = Plan(n, torch.int32, device=dev)
     useful = 8.0 * n + 8.0 * (S + 1)
+    bounds = [(int(offs[i]), int(offs[i + 1])) for i in range(S) if offs[i + 1] > offs[i]]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(3):
+
+    def batched():
         plan.run_segmented(x, d_off, out=out)
-    plan.check()
-    ts = []
-    for _ in range(7):
-        e0.record()
-        plan.run_segmented(x, d_off, out=out)
-        e1.record()
-        plan.check()
-        ts.append(e0.elapsed_time(e1))
-    batched_ms = statistics.median(ts)
-    bounds = [(int(offs[i]), int(offs[i + 1])) for i in range(S)]
-    loop_ts = []
-    for _ in range(2):
-        torch.cuda.synchronize(dev)
-        e0.record()
+
+    def loop():
         for a, b in bounds:
-            if b > a:
-                plan.run(x[a:b], out=out[a:b])
-        e1.record()
+            plan.run(x[a:b], out=out[a:b])
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
         plan.check()
-        loop_ts.append(e0.elapsed_time(e1))
-    loop_ms = min(loop_ts)
+        return ts
+
+    side = torch.cuda.Stream(device=dev)
+    graphs = {}
+    for name, fn in (("batched", batched), ("loop", loop)):
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            fn()  # warm-up (plans pick their configurations; nothing is allocated in a run)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            fn()
+        graphs[name] = g
+    batched_ms = statistics.median(timed(graphs["batched"].replay, 7))
+    loop_ms = min(timed(graphs["loop"].replay, 3))
+    loop_py_ms = min(timed(loop, 2))
     plan.close()
     return {"workload": "batch_4096_loguniform_32_2p20_int32", "segments": S, "keys": n,
             "useful_bytes": int(useful), "batched_ms": round(batched_ms, 4), "loop_ms": round(loop_ms, 3),
+            "loop_ms_python_enqueue": round(loop_py_ms, 3),
             "batched_gbs": round(useful / batched_ms / 1e6, 1), "loop_gbs": round(useful / loop_ms / 1e6, 2),
-            "speedup_vs_loop": round(loop_ms / batched_ms, 2), "launches": {"batched": 1, "loop": S},
-            "note": "device time (CUDA events); the loop is enqueued from Python, one apsep_run per array"}
+            "speedup_vs_loop": round(loop_ms / batched_ms, 2), "launches": {"batched": 1, "loop": len(bounds)},
+            "note": "device time (CUDA events) of graph replays: the batch as one captured launch, the loop as "
+                    "one captured graph of one apsep_run per array"}
 
 
 def run_consumers(dev, peak_gbs: float) -> dict:
