@@ -45,6 +45,7 @@ SIGNATURES = {
 }
 
 NOALLOC_MAX_KEYS = 4194304  # APSEP_NOALLOC_MAX_KEYS in include/apsep.h
+NUM_CONFIGS = 6  # kernel configurations of the 4-byte key engine (apsep_num_configs)
 MAX_KEYS = 2147479552  # APSEP_MAX_KEYS in include/apsep.h (2^31 - 4096)
 MAX_KEYS64 = 1 << 40  # APSEP_MAX_KEYS64 in include/apsep.h
 

@@ -55,7 +55,7 @@ struct RangeScratch {
 constexpr int kMinTileKeys = 256;   // smallest tile of any configuration (one warp's)
 constexpr int kMaxTileKeys = 512;   // largest tile of any configuration
 constexpr int kMaxRanges = 4096;    // persistent warps per run, upper bound
-constexpr int kMaxCtas = kMaxRanges / 8;  // every configuration runs >= 8 warps per CTA
+constexpr int kMaxCtas = kMaxRanges / 4;  // every configuration runs >= 4 warps per CTA
 constexpr int kReadyStride = 16;          // words between two CTAs' ready flags (64 bytes)
 constexpr int kTopEntries = 32;           // stack entries each range publishes for later ranges
 
@@ -127,7 +127,7 @@ struct TileConfig {
     int wpc;
     int ipt;
 };
-constexpr int kNumTileConfigs = 2;
+constexpr int kNumTileConfigs = 6;
 extern const TileConfig kTileConfigs[kNumTileConfigs];
 
 // Launch one run.  Fills a.num_ranges / a.tiles_per_range from the

@@ -8,7 +8,7 @@
 // the scratch this engine needs (control block, look-back words, tile and
 // chunk minima) lives in one file-scope __device__ array below, sized for at
 // most APSEP_NOALLOC_MAX_KEYS keys.  Every GPU that loads this library holds
-// that array (2,869,504 bytes) until the process exits.
+// that array (2,902,272 bytes) until the process exits.
 //
 // Host code must not pass the array's name to a kernel: on the host it is
 // only a stand-in symbol.  Every call looks up the array's device address
@@ -35,7 +35,7 @@ namespace {
 
 constexpr int64_t kMaxKeys = APSEP_NOALLOC_MAX_KEYS;
 constexpr size_t kBytes = scratch_offsets(kMaxKeys).total;  // the same layout a plan uses
-static_assert(kBytes == 2869504, "the size stated in include/apsep.h changed: update it there");
+static_assert(kBytes == 2902272, "the size stated in include/apsep.h changed: update it there");
 
 constexpr int kConfig = 0;                 // 16 warps per CTA, 512-key warp tiles
 constexpr uint32_t kSpinLimit = 1u << 22;  // bound on every device-side wait

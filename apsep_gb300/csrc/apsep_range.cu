@@ -8,7 +8,11 @@ namespace apsep {
 
 const TileConfig kTileConfigs[kNumTileConfigs] = {
     {16, 16},  // 16 warps per CTA (one CTA per SM), 512-key warp tiles
-    {8, 8},   // 8 warps per CTA, 256-key warp tiles
+    {8, 8},    // 8 warps per CTA, 256-key warp tiles
+    {8, 16},   // 8 warps per CTA, 512-key warp tiles
+    {16, 8},   // 16 warps per CTA, 256-key warp tiles
+    {4, 16},   // 4 warps per CTA: a small array spreads over more SMs
+    {4, 8},
 };
 
 size_t carve_scratch(void* base, int64_t capacity, RangeScratch* s, int kb) {

@@ -266,11 +266,17 @@ __device__ __noinline__ int nearest_range(T q, int hi, const RangeArgs& a) {
 // start order), so no wait depends on a warp that may not start.  Every wait
 // is bounded and reports ERR_LOOKBACK_TIMEOUT when it gives up.
 // ---------------------------------------------------------------------------
+// A launch of at most kDirectRanges ranges skips the global step: range r polls
+// the tagged minima of the ranges before it directly (a few words), which ends
+// sooner than waiting for every range of the launch to publish.
+constexpr int kDirectRanges = 256;
+
 template <typename T>
 __device__ void range_publish(int r, uint32_t epoch, T rmin, const RangeArgs& a) {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t tag = (epoch << 2) | FLAG_AGG;
+    const bool direct = a.num_ranges <= kDirectRanges;
     int last = 0;
     if (lane == 0 && r != a.skip_publish_range) {
         if constexpr (sizeof(T) == 8)
@@ -282,8 +288,10 @@ __device__ void range_publish(int r, uint32_t epoch, T rmin, const RangeArgs& a)
         __threadfence();
         __stcg((unsigned long long*)&a.s.range_state[r],
                ((uint64_t)tag << 32) | (sizeof(T) == 8 ? 0u : (uint32_t)KeyTraits<T>::bits(rmin)));
-        last = atomicAdd(&a.s.ctr->finished, 1u) == (uint32_t)(a.num_ranges - 1);
-        if (last) __threadfence();  // acquire: every range's publication
+        if (!direct) {
+            last = atomicAdd(&a.s.ctr->finished, 1u) == (uint32_t)(a.num_ranges - 1);
+            if (last) __threadfence();  // acquire: every range's publication
+        }
     }
     if (!__shfl_sync(FULL, last, 0)) return;
     __syncwarp();
@@ -330,9 +338,10 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
         for (int o = 16; o > 0; o >>= 1) m = KeyTraits<T>::vmin(m, __shfl_xor_sync(FULL, m, o));
         p = m;
     };
-    // 1. the ready flag of this CTA (one line, polled by one lane per warp)
+    // 1. the ready flag of this CTA (one line, polled by one lane per warp); a
+    //    launch of few ranges raises none: its ranges wait on their predecessors
     int ready = 0;
-    if (lane == 0) {
+    if (lane == 0 && a.num_ranges > kDirectRanges) {
         const uint32_t bound = min(a.spin_limit, 1u << 16);
         for (uint32_t s = 0;; s++) {
             if (ld_acquire_u32(flag) == epoch) {
@@ -1543,6 +1552,10 @@ inline cudaError_t prepare_mode(int cfg, int* per_sm) {
     switch (cfg) {
     case 0: P_(16, 16); break;
     case 1: P_(8, 8); break;
+    case 2: P_(16, 8); break;
+    case 3: P_(8, 16); break;
+    case 4: P_(16, 4); break;
+    case 5: P_(8, 4); break;
     default: return cudaErrorInvalidValue;
     }
 #undef P_
@@ -1562,6 +1575,10 @@ inline cudaError_t launch_mode(int dtype, int incl, int cfg, RangeArgs& a, const
     switch (cfg) {
     case 0: L_(16, 16);
     case 1: L_(8, 8);
+    case 2: L_(16, 8);
+    case 3: L_(8, 16);
+    case 4: L_(16, 4);
+    case 5: L_(8, 4);
     }
 #undef L_
     return cudaErrorInvalidValue;

@@ -153,7 +153,7 @@ apsep_status apsep_launch(const void* d_in, int32_t* d_out, int64_t n, apsep_dty
  * synchronisation are not allowed).  No counterpart in the reference: its
  * every entry point allocates or takes caller-allocated scratch.
  * The scratch is a static device array sized for APSEP_NOALLOC_MAX_KEYS keys
- * (2,869,504 bytes, held on every GPU that loads the library until exit);
+ * (2,902,272 bytes, held on every GPU that loads the library until exit);
  * n > APSEP_NOALLOC_MAX_KEYS returns APSEP_EINVAL; a device below compute
  * capability 10 returns APSEP_ENOTSUP.  Every call looks up the array's
  * address (a lookup that allocates nothing); the first call in each CUDA

@@ -44,7 +44,7 @@ def test_status_strings_and_configs(built_lib):
     assert lib.apsep_status_string(_lib.APSEP_OK) == b"ok"
     assert lib.apsep_status_string(_lib.APSEP_ETIMEOUT) == b"device-side wait timed out"
     n = lib.apsep_num_configs()
-    assert n >= 1
+    assert n == _lib.NUM_CONFIGS
     for c in range(n):
         t, k = ctypes.c_int32(), ctypes.c_int32()
         assert lib.apsep_config_shape(c, ctypes.byref(t), ctypes.byref(k)) == _lib.APSEP_OK

@@ -160,7 +160,7 @@ def test_float_segments(le):
         check(plan, a, offs, le)
 
 
-@pytest.mark.parametrize("config", [0, 1])
+@pytest.mark.parametrize("config", range(_lib.NUM_CONFIGS))
 def test_every_config(config):
     rng = np.random.default_rng(17 + config)
     lengths = list(rng.integers(0, 40000, 60)) + EDGE_LENGTHS

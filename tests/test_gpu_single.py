@@ -146,7 +146,7 @@ def near_monotone(n, kind, ipt):
     return a.astype(np.int32)
 
 
-@pytest.mark.parametrize("config", [0, 1])
+@pytest.mark.parametrize("config", range(_lib.NUM_CONFIGS))
 @pytest.mark.parametrize("kind", ["asc_dip", "desc_bump", "asc_ties", "asc_rare_tie"])
 @pytest.mark.parametrize("le", [False, True])
 def test_near_monotone_tiles(config, kind, le):
@@ -162,7 +162,7 @@ def test_near_monotone_tiles(config, kind, le):
         pytest.fail("first mismatch at %d: got %d want %d" % (bad, got[bad], want[bad]))
 
 
-@pytest.mark.parametrize("config", [0, 1])
+@pytest.mark.parametrize("config", range(_lib.NUM_CONFIGS))
 def test_every_config(config):
     rng = np.random.default_rng(77 + config)
     with Plan(300000, torch.int32) as plan:
