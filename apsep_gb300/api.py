@@ -80,7 +80,7 @@ class Plan:
     def _tune_for(self, n: int) -> None:
         if self._tuning is None:
             return
-        cfg = self._tuning.config_for(n)
+        cfg = self._tuning.config_for(n, self.dtype)
         if cfg is not None and cfg != self._cfg:
             _lib.check(self._lib.apsep_plan_set_config(self._h, int(cfg)), "apsep_plan_set_config")
             self._cfg = cfg

@@ -1,8 +1,9 @@
 """Autotuner: the kernel configuration per size class, measured on this GPU.
 
-The engine has one tunable knob, the kernel configuration (warps per CTA x
-keys per lane, `apsep_num_configs()` of them; there is no cluster dimension:
-ranges are warp-independent).  A size class is floor(log2(n)); the tuner
+The engine has one tunable knob, the kernel configuration: warps per CTA
+{4, 8, 16} x keys per lane {8, 16} (`apsep_num_configs()` of them; 32 keys per
+lane would double the in-lane compare ladder's cost per key, and there is no
+cluster dimension: ranges are warp-independent).  A size class is floor(log2(n)); the tuner
 times every configuration on seeded synthetic arrays of that size (uniform,
 descending and ascending keys, the single-array benchmark's inputs), keeps the
 one with the lowest total time, and stores {class: config} in a table.  A
@@ -43,25 +44,38 @@ def config_shape(config: int) -> tuple[int, int]:
 
 
 class Table:
-    """{size class: configuration}; classes outside the table use the nearest one."""
+    """{size class: configuration} (for int32 keys, and per other key type in
+    `by_dtype`); classes outside the table use the nearest one.  `timings`
+    keeps the measured microseconds per run of every configuration."""
 
-    def __init__(self, entries: dict[int, int], device_name: str = ""):
+    def __init__(self, entries: dict[int, int], device_name: str = "", by_dtype: dict | None = None,
+                 timings: dict | None = None):
         self.entries = {int(k): int(v) for k, v in entries.items()}
         self.device_name = device_name
+        self.by_dtype = {str(d): {int(k): int(v) for k, v in e.items()} for d, e in (by_dtype or {}).items()}
+        self.timings = timings or {}
 
-    def config_for(self, n: int) -> int | None:
-        if not self.entries:
+    def config_for(self, n: int, dtype=None) -> int | None:
+        name = str(dtype).replace("torch.", "") if dtype is not None else "int32"
+        entries = self.by_dtype.get(name) or self.entries
+        if not entries:
             return None
         c = size_class(n)
-        best = min(self.entries, key=lambda k: (abs(k - c), k))
-        return self.entries[best]
+        best = min(entries, key=lambda k: (abs(k - c), k))
+        return entries[best]
 
     def to_json(self) -> dict:
-        return {"device": self.device_name, "classes": {str(k): v for k, v in sorted(self.entries.items())}}
+        d = {"device": self.device_name, "classes": {str(k): v for k, v in sorted(self.entries.items())}}
+        if self.by_dtype:
+            d["by_dtype"] = {t: {str(k): v for k, v in sorted(e.items())} for t, e in self.by_dtype.items()}
+        if self.timings:
+            d["timings_us"] = self.timings
+        return d
 
     @staticmethod
     def from_json(d: dict) -> "Table":
-        return Table({int(k): int(v) for k, v in d.get("classes", {}).items()}, d.get("device", ""))
+        return Table({int(k): int(v) for k, v in d.get("classes", {}).items()}, d.get("device", ""),
+                     d.get("by_dtype"), d.get("timings_us"))
 
 
 def save(table: Table, path: str) -> None:
@@ -97,12 +111,13 @@ def tune(dtype: torch.dtype = torch.int32, classes=range(14, 27), reps: int = 5,
     nmax = 1 << max(classes)
     plan = Plan(nmax, dtype, inclusive=inclusive, device=dev)
     out = torch.empty(nmax, dtype=torch.int32, device=dev)
-    entries = {}
+    entries, timings = {}, {}
     try:
         for c in classes:
             n = 1 << c
             xs = _inputs(n, dtype, dev)
             best, best_t = 0, float("inf")
+            per = {}
             for cfg in range(num_configs()):
                 plan.set_config(cfg)
                 for x in xs:  # warm-up
@@ -116,11 +131,21 @@ def tune(dtype: torch.dtype = torch.int32, classes=range(14, 27), reps: int = 5,
                 e1.record()
                 plan.check()
                 t = e0.elapsed_time(e1)
+                per[cfg] = t * 1e3 / (reps * len(xs))
                 if verbose:
                     print("class %d config %d: %.1f us per run" % (c, cfg, t * 1e3 / (reps * len(xs))))
                 if t < best_t:
                     best, best_t = cfg, t
             entries[c] = best
+            timings[str(c)] = {str(k): round(v, 2) for k, v in per.items()}
     finally:
         plan.close()
-    return Table(entries, torch.cuda.get_device_name(dev))
+    return Table(entries, torch.cuda.get_device_name(dev), timings={str(dtype).replace("torch.", ""): timings})
+
+
+def tune_all(classes=range(14, 31), reps: int = 5, device=None, verbose: bool = False) -> Table:
+    """tune() for int32 and float32 keys; one table (int32 entries as the default)."""
+    t_i = tune(torch.int32, classes, reps, device=device, verbose=verbose)
+    t_f = tune(torch.float32, classes, reps, device=device, verbose=verbose)
+    return Table(t_i.entries, t_i.device_name, by_dtype={"float32": t_f.entries},
+                 timings={**t_i.timings, **t_f.timings})
