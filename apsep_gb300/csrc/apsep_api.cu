@@ -25,7 +25,6 @@ struct apsep_plan {
     RangeScratch rs{};
     int dbg_skip_range = -1;
     uint32_t dbg_spin_limit = 0;
-    int last_head = 0;  // view head of the last single-array run (its chunk minima sit shifted by it)
 };
 
 namespace {
@@ -96,8 +95,6 @@ bool ranges_overlap(const void* a, size_t an, const void* b, size_t bn) {
 
 }  // namespace
 
-uint32_t* plan_error_word(apsep_plan* p) { return &p->rs.ctr->err; }
-const void* plan_chunk_minima(apsep_plan* p) { return p->last_head == 0 ? p->rs.chunk_min : nullptr; }
 
 extern "C" {
 
@@ -250,7 +247,6 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
         a.s = p->rs;
         p->dbg_skip_range = -1;
         p->dbg_spin_limit = 0;
-        p->last_head = 0;
         const cudaError_t e = launch_range_wide(p->dtype, cmp == APSEP_LE ? 1 : 0, a, mi, mo, (cudaStream_t)stream);
         return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
     }
@@ -292,7 +288,6 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
     a.s = p->rs;
     p->dbg_skip_range = -1;  // one-shot
     p->dbg_spin_limit = 0;
-    p->last_head = head;
     const int incl = cmp == APSEP_LE ? 1 : 0;
     cudaError_t e = offsets ? launch_range_segmented(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
                     : head  ? launch_range_view(p->dtype, incl, p->cfg, a, mi, mo, (cudaStream_t)stream)
@@ -301,6 +296,46 @@ apsep_status run_impl(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n
 }
 
 }  // namespace
+
+apsep_status plan_run_out64(apsep_plan* p, const void* d_in, int64_t* d_out, int64_t n, int64_t out_base,
+                            apsep_cmp cmp, void* chunk_min, void* stream, RangeArgs* layout) {
+    if (!p || !layout || n <= 0 || n > p->capacity || !d_in || !d_out || (cmp != APSEP_LT && cmp != APSEP_LE))
+        return APSEP_EINVAL;
+    const int kb = key_bytes(p->dtype);
+    if ((uintptr_t)d_in % kb != 0 || (uintptr_t)d_out % 8 != 0 || (chunk_min && (uintptr_t)chunk_min % kb != 0))
+        return APSEP_EINVAL;
+    DeviceGuard g(p->device);
+    if (!g.ok) return APSEP_ECUDA;
+    const int B = wide(p->dtype) ? kWideTileKeys : 32 * kTileConfigs[0].ipt;  // keys per warp tile
+    const int tile_rows = B * kb / 128;                                         // 128-byte rows per tile
+    int rows = (int)(n * kb / 128);
+    CUtensorMap mi;
+    memset(&mi, 0, sizeof(mi));
+    if ((uintptr_t)d_in % 16 != 0 || rows < tile_rows) rows = 0;
+    if (rows > 0 && !encode_rows(&mi, d_in, rows, tile_rows, p->dtype)) return APSEP_ECUDA;
+    RangeArgs a;
+    a.d_in = d_in;
+    a.d_out = nullptr;
+    a.n = (int)n;
+    a.head = 0;
+    a.num_tiles = (int)((n + B - 1) / B);
+    a.tiles_per_range = 0;
+    a.num_ranges = 0;
+    a.tma_rows = rows;
+    a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
+    a.skip_publish_range = p->dbg_skip_range;
+    a.offsets = nullptr;
+    a.nseg = 1;
+    a.s = p->rs;
+    if (chunk_min) a.s.chunk_min = chunk_min;
+    a.d_out64 = d_out;
+    a.out_base = out_base;
+    p->dbg_skip_range = -1;
+    p->dbg_spin_limit = 0;
+    const cudaError_t e = launch_range_out64(p->dtype, cmp == APSEP_LE ? 1 : 0, a, mi, (cudaStream_t)stream);
+    *layout = a;
+    return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
+}
 
 extern "C" {
 

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "apsep.h"
+
 namespace apsep {
 
 // Error bits in Counters::err (read back by apsep_plan_check).
@@ -110,7 +112,16 @@ struct RangeArgs {
     const int64_t* offsets;  // segmented runs: nseg + 1 segment offsets into d_in; else nullptr
     int nseg;
     RangeScratch s;
+    int64_t* d_out64 = nullptr;  // int64 answers (the int64-position path's kernels): out_base + answer
+    int64_t out_base = 0;
 };
+
+// Runs with int64 answers (RangeArgs::d_out64): a key that no key of the run
+// answers reads UNRESOLVED64, and a tile whose keys are all unanswered within
+// their range is not written at all; its tile_flag word carries
+// TILE_NOT_STORED (phase 2 still writes the keys that it answers).
+constexpr int64_t UNRESOLVED64 = -2;
+constexpr uint32_t TILE_NOT_STORED = 0x40000000u;
 
 // The TMA view of a run: the number of virtual keys (0..3) in front of d_in
 // that put the view on a 16-byte boundary, or -1 when the input and the output
@@ -153,16 +164,21 @@ cudaError_t launch_range_view(int dtype, int incl, int cfg, RangeArgs& a, const 
                               const CUtensorMap& map_out, cudaStream_t st);
 cudaError_t prepare_segmented(int cfg, int* ctas_per_sm);
 cudaError_t range_max_warps(int cfg, int* warps);  // persistent warps of one launch, current device
+// A single array (no view head) with int64 answers a.out_base + answer into
+// a.d_out64 (4-byte keys in configuration 0, 8-byte keys in theirs); flagged keys
+// get UNRESOLVED64 and all-deferred tiles are not written (TILE_NOT_STORED).
+cudaError_t launch_range_out64(int dtype, int incl, RangeArgs& a, const CUtensorMap& map_in, cudaStream_t st);
 // Arms one-shot fault injection for the next apsep_run_noalloc call.
 void noalloc_debug_inject(int32_t range, uint32_t spin_limit);
 
 }  // namespace apsep
 
-// The plan's sticky device-side error word (ERR_* bits, read by
-// apsep_plan_check), for passes that run around the engine.
 struct apsep_plan;
-uint32_t* plan_error_word(struct apsep_plan* plan);
-// The minimum of every 32 keys of the plan's last single-array run (written
-// by its phase 1, in key order), or null when that run sat behind a view
-// head (its chunks then start `head` keys before the array).
-const void* plan_chunk_minima(struct apsep_plan* plan);
+// One single-array run of the plan with int64 answers (out_base + answer into
+// d_out; see launch_range_out64): 4-byte keys in configuration 0, 8-byte keys
+// in theirs, tiles by TMA when d_in is 16-byte aligned, else by plain loads.
+// chunk_min, when not null, takes the run's minima of every 32 keys (in key
+// order, up to the end of the last tile) instead of the plan's scratch.
+// *layout returns the run's arguments: tile and range layout, scratch words.
+apsep_status plan_run_out64(struct apsep_plan* plan, const void* d_in, int64_t* d_out, int64_t n, int64_t out_base,
+                            apsep_cmp cmp, void* chunk_min, void* stream, apsep::RangeArgs* layout);

@@ -389,7 +389,13 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
 
 // MAPF: int64 key slots that hold float64 bit patterns, compared through
 // f64_order (keys are mapped as they enter shared memory or registers).
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false>
+// OUT64 (single arrays, no view head): answers as int64, a.out_base + answer,
+// into a.d_out64, for the int64-position path: a flagged key gets UNRESOLVED64
+// (phase 2 overwrites the ones it answers), and a tile whose keys are all
+// deferred is not written at all (its flag word says so); the int64-position
+// path answers what is left.
+
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false, bool OUT64 = false>
 __global__ void __launch_bounds__(WPC * 32, (WPC >= 16 && sizeof(T) == 4 ? 1 : 2))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
@@ -440,6 +446,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         return a.offsets ? (int64_t)__ldg(&a.offsets[i]) : (i == 0 ? (int64_t)0 : (int64_t)(a.n - head));
     };
     auto seg_idx = [&](int pos) { return a.offsets ? seg_find(a.offsets, a.nseg, pos, err) : 0; };
+    static_assert(!OUT64 || (!SEG && EP), "int64 answers: single arrays only");
+    // a final answer v of position pos (phase 2); int64 answers: out_base + v, and
+    // UNRESOLVED64 for none (the key is left to the int64-position path)
+    auto put = [&](int pos, int v) {
+        if constexpr (OUT64) a.d_out64[pos] = v >= 0 ? (int64_t)v + a.out_base : UNRESOLVED64;
+        else a.d_out[pos] = v;
+    };
 
     // One claim per CTA: its warps take WPC consecutive range ids, in the order
     // the CTAs start (so every range a warp may wait on belongs to a started CTA).
@@ -645,6 +658,18 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             // The whole tile leaves O, flagged keys as -1 (segmented runs: answers made
             // relative to their segment's start).
             auto store_tile = [&]() {
+                if constexpr (OUT64) {  // int64 answers, 32 consecutive keys per store
+                    __syncwarp();       // every lane's answers are in O
+#pragma unroll
+                    for (int j = 0; j < IPT; j++) {
+                        const int e = j * 32 + lane;
+                        if (e < valid_keys) {
+                            const int o = O[swz(e)];
+                            a.d_out64[tile_base + e] = o >= 0 ? (int64_t)o + a.out_base : UNRESOLVED64;
+                        }
+                    }
+                    return;
+                }
                 if constexpr (SEG) {  // answers relative to their segment's start
                     __syncwarp();     // every lane's answers are in O
     #pragma unroll
@@ -726,21 +751,23 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     }
                     if (lane < W) __stcg(&a.s.tile_mask[(size_t)t * MW + lane], 0xffffffffu);
                     if (lane == 0) {
-                        __stcg(&a.s.tile_flag[t], (uint32_t)WT);
+                        __stcg(&a.s.tile_flag[t], (uint32_t)WT | (OUT64 ? TILE_NOT_STORED : 0u));
                         __stcg(&tile_min_w[t], tmin);
                     }
                     def_total += WT;
-                    fence_proxy_async_smem();
-                    __syncwarp();
-                    if (full) {
-                        if (lane == 0) {
-                            tma_store_2d(&map_out, 0, t * W, O);
-                            bulk_commit();
-                        }
-                    } else {
+                    if constexpr (!OUT64) {  // (int64 answers: the tile is left to the int64-position path)
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (full) {
+                            if (lane == 0) {
+                                tma_store_2d(&map_out, 0, t * W, O);
+                                bulk_commit();
+                            }
+                        } else {
 #pragma unroll
-                        for (int j = 0; j < IPT; j++)
-                            if (!head || tile_base + j * 32 + lane >= head) a.d_out[tile_base + j * 32 + lane] = -1;
+                            for (int j = 0; j < IPT; j++)
+                                if (!head || tile_base + j * 32 + lane >= head) a.d_out[tile_base + j * 32 + lane] = -1;
+                        }
                     }
                     if (lane == 31) {
                         sStkV[stk_lo & (K - 1)] = v[IPT - 1];
@@ -792,18 +819,22 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         __stcg(&a.s.tile_flag[t], 0u);
                         __stcg(&tile_min_w[t], first);
                     }
-                    fence_proxy_async_smem();
-                    __syncwarp();
-                    if (full) {
-                        if (lane == 0) {
-                            tma_store_2d(&map_out, 0, t * W, O);
-                            bulk_commit();
-                        }
+                    if constexpr (OUT64) {
+                        store_tile();
                     } else {
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (full) {
+                            if (lane == 0) {
+                                tma_store_2d(&map_out, 0, t * W, O);
+                                bulk_commit();
+                            }
+                        } else {
 #pragma unroll
-                        for (int j = 0; j < IPT; j++)
-                            if (!head || tile_base + j * 32 + lane >= head)
-                                a.d_out[tile_base + j * 32 + lane] = O[swz(j * 32 + lane)];
+                            for (int j = 0; j < IPT; j++)
+                                if (!head || tile_base + j * 32 + lane >= head)
+                                    a.d_out[tile_base + j * 32 + lane] = O[swz(j * 32 + lane)];
+                        }
                     }
                     const int base_idx = stk_hi;  // entry of tile key e: base_idx + e
 #pragma unroll
@@ -1378,7 +1409,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             }
             if (want) {
                 if (ans < 0) atomicOr(err, ERR_INTERNAL);
-                else if (!head || pos >= head) a.d_out[pos] = SEG ? seg_rel(ans, first_start) : ans;
+                else if (!head || pos >= head) put(pos, SEG ? seg_rel(ans, first_start) : ans);
             }
         }
         if (!a_done && def_total > kDefCap) {
@@ -1409,7 +1440,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
                             if (lane == f) {
                                 if (found < -1) atomicOr(err, ERR_INTERNAL);
-                                else a.d_out[pos] = SEG ? seg_rel(found, sf) : found;
+                                else put(pos, SEG ? seg_rel(found, sf) : found);
                             }
                         }
                         continue;
@@ -1425,7 +1456,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         const unsigned ok = __ballot_sync(FULL, ((pend >> lane) & 1u) && cur >= 0 && lt<INCL>(cv, q));
                         const unsigned fail = pend & ~ok;
                         const unsigned tk = fail ? (pend & ((fail & (0u - fail)) - 1u)) : pend;
-                        if ((tk >> lane) & 1u) a.d_out[pos] = SEG ? seg_rel(cur, first_start) : cur;
+                        if ((tk >> lane) & 1u) put(pos, SEG ? seg_rel(cur, first_start) : cur);
                         pend &= ~tk;
                         if (!pend) break;
                         const int f = __ffs(pend) - 1;
@@ -1453,7 +1484,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                                                            chunk_min_r, a);
             if (lane == 0) {
                 if (found < 0) atomicOr(err, ERR_INTERNAL);
-                else if (!head || pos >= head) a.d_out[pos] = SEG ? seg_rel(found, sCapS[j]) : found;
+                else if (!head || pos >= head) put(pos, SEG ? seg_rel(found, sCapS[j]) : found);
             }
         }
         if (cap_total > kCapCap) {
@@ -1476,7 +1507,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
                         if (lane == f) {
                             if (found < -1) atomicOr(err, ERR_INTERNAL);
-                            else a.d_out[pf] = SEG ? seg_rel(found, sf) : found;
+                            else put(pf, SEG ? seg_rel(found, sf) : found);
                         }
                     }
                 }
@@ -1510,7 +1541,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 // ---------------------------------------------------------------------------
 // Launch plumbing shared by the single-array and segmented translation units.
 // ---------------------------------------------------------------------------
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false, bool OUT64 = false>
 inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo, cudaStream_t st,
                             int max_warps) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
@@ -1519,14 +1550,14 @@ inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorM
     a.tiles_per_range = tpr;
     a.num_ranges = (a.num_tiles + tpr - 1) / tpr;
     const int ctas = (a.num_ranges + WPC - 1) / WPC;
-    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
+    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUT64><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
     return cudaGetLastError();
 }
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false, bool OUT64 = false>
 inline cudaError_t prepare_t(int* ctas_per_sm) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
-    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF>;
+    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUT64>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int n = 0;

@@ -9,7 +9,7 @@ Allocates one input and one output ((4 or 8) * n + 4 * n bytes), runs `reps` APS
 launches with a synchronisation after each, prints the last launch's time.
 With --piece, each rep is one Plan.run64 (int64 positions, 8 * n bytes of
 answers) on a plan of that capacity, so the array runs as pieces of that
-many keys (engine run + widening pass per piece).
+many keys (engine run + fix-up pass per piece).
 Small enough on the device for ncu captures; n = 2^25 keeps the 128 MiB
 input above the 126 MiB L2.
 """

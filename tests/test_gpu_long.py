@@ -82,9 +82,8 @@ def test_pieces_against_the_oracle(plans, name, dtype):
 
 @pytest.mark.parametrize("dtype", TYPES, ids=lambda t: t.__name__)
 def test_pieces_off_a_16_byte_boundary(plans, dtype):
-    # keys one element past an aligned base: 4-byte keys run each piece behind
-    # a view head (level-1 minima then come from the keys themselves), 8-byte
-    # keys without TMA; answers to an 8-byte aligned int64 buffer
+    # keys one element past an aligned base: every piece's tiles come by plain
+    # loads instead of TMA; answers to an 8-byte aligned int64 buffer
     rng = np.random.default_rng(90 + TYPES.index(dtype))
     n = 60_007
     for name in ("uniform", "rising_runs", "walk"):
