@@ -1416,19 +1416,72 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             // A'. the list overflowed and P qualified every listed key: continue over
             //     the tile flags after the last listed key, with a monotone cursor
             //     (answers of non-increasing queries only move left).
+            //     Flag words 32 tiles per load (lane i: tile tb + i), a tile's mask
+            //     words in one load (lane w: word w): the scan pays one L2 round
+            //     trip per 32 tiles and one per flagged tile, not one per tile and word.
             const int from = sDefP[kDefCap - 1] + 1;
             int cur = -1;
             T cv = KeyTraits<T>::pad();
-            for (int t = from / WT; t < t1 && !a_done; t++) {
-                const uint32_t tf = __ldcg(&a.s.tile_flag[t]);
-                if ((tf & 0x7fffffffu) == 0) continue;
-                const bool mixed = (tf >> 31) != 0;
+            static_assert(W <= 16, "two tiles' mask words per load");
+            for (int tb = from / WT; tb < t1 && !a_done; tb += 32) {
+              const bool tin = tb + lane < t1;
+              const uint32_t tfl = tin ? __ldcg(&a.s.tile_flag[tb + lane]) : 0u;
+              const T tmn = tin ? __ldcg(&tile_min_r[tb + lane]) : KeyTraits<T>::pad();
+              unsigned fl = __ballot_sync(FULL, (tfl & 0x7fffffffu) != 0);
+              while (fl && !a_done) {
+                // Flagged tiles whose pending keys all take the cursor: not mixed, and
+                // P and the cursor's key both qualify for the tile's minimum (<= every
+                // pending key).  Pending keys do not increase, so these form a prefix
+                // of the flagged tiles; their keys are not read, and the mask words of
+                // two tiles come in one load (lanes 0-15 and 16-31).
+                const unsigned fast = __ballot_sync(
+                    FULL, ((fl >> lane) & 1u) && (tfl >> 31) == 0 && cur >= 0 && lt<INCL>(P, tmn) && lt<INCL>(cv, tmn));
+                const unsigned slow = fl & ~fast;
+                unsigned take = slow ? fl & ((slow & (0u - slow)) - 1u) : fl;
+                fl &= ~take;
+                while (take) {
+                    const int ta = __ffs(take) - 1;
+                    take &= take - 1;
+                    const int tb2 = take ? __ffs(take) - 1 : -1;
+                    if (take) take &= take - 1;
+                    const int mine = lane < 16 ? ta : tb2;
+                    const uint32_t mw2 =
+                        mine >= 0 && (lane & 15) < W ? __ldcg(&a.s.tile_mask[(size_t)(tb + mine) * MW + (lane & 15)]) : 0u;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int tt = h ? tb2 : ta;
+                        if (tt < 0) break;
+#pragma unroll
+                        for (int w = 0; w < W; w++) {
+                            const uint32_t mw = __shfl_sync(FULL, mw2, 16 * h + w);
+                            const int pos = (tb + tt) * WT + w * 32 + lane;
+                            if (((mw >> lane) & 1u) && pos >= from && (!head || pos >= head))
+                                put(pos, SEG ? seg_rel(cur, first_start) : cur);
+                        }
+                    }
+                }
+                if (!fl) break;
+                // the first other flagged tile, key by key
+                const int fsrc = __ffs(fl) - 1;
+                fl &= fl - 1;
+                const int t = tb + fsrc;
+                const bool mixed = (__shfl_sync(FULL, tfl, fsrc) >> 31) != 0;
+                const uint32_t mwl = lane < W ? __ldcg(&a.s.tile_mask[(size_t)t * MW + lane]) : 0u;
+                // The tile's pending keys, every word's loads in flight together, staged
+                // in the idle TMA ring (each lane reads back only its own slots).
+#pragma unroll
+                for (int w = 0; w < W; w++) {
+                    const uint32_t mw = __shfl_sync(FULL, mwl, w);
+                    const int pos = t * WT + w * 32 + lane;
+                    const bool pk = ((mw >> lane) & 1u) && pos >= from && (!head || pos >= head);
+                    sV[w * 32 + lane] = pk ? load_key<T, MAPF>(&d_in[pos]) : KeyTraits<T>::pad();
+                }
                 for (int w = 0; w < W && !a_done; w++) {
-                    const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
+                    const uint32_t mw = __shfl_sync(FULL, mwl, w);
                     const int pos = t * WT + w * 32 + lane;
                     unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from && (!head || pos >= head));
                     if (!pend) continue;
-                    const T q = ((pend >> lane) & 1u) ? load_key<T, MAPF>(&d_in[pos]) : KeyTraits<T>::pad();
+                    const T q = ((pend >> lane) & 1u) ? sV[w * 32 + lane] : KeyTraits<T>::pad();
                     if (mixed) {  // deferred and capped keys: a full search each
                         while (pend) {
                             const int f = __ffs(pend) - 1;
@@ -1461,8 +1514,24 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         if (!pend) break;
                         const int f = __ffs(pend) - 1;
                         const T qf = __shfl_sync(FULL, q, f);
-                        const int found = find_left<T, WT, INCL, MAPF>(qf, cur >= 0 ? cur : range_begin, d_in, tile_min_r,
-                                                                 chunk_min_r, a);
+                        // qf's answer lies before the range: in the nearest earlier range
+                        // whose minimum qualifies (the window, else the group minima), at
+                        // the topmost qualifying entry of that range's final stack (every
+                        // key after it there is >= qf); find_left when the published top
+                        // part does not reach it
+                        int found = -2;
+                        {
+                            const unsigned wm = __ballot_sync(FULL, r - 1 - lane >= 0 && lt<INCL>(win, qf));
+                            const int rpf = wm ? r - 1 - (__ffs(wm) - 1) : nearest_range<T, INCL>(qf, r - 33, a);
+                            if (rpf >= 0) {
+                                const int cnt = (int)(__ldcg(&a.s.top_cnt[rpf]) & 0xffu);
+                                const T tkey = lane < cnt ? __ldcg(&((const T*)a.s.top_key)[(size_t)rpf * kTopEntries + lane])
+                                                          : KeyTraits<T>::pad();
+                                const unsigned m = __ballot_sync(FULL, lane < cnt && lt<INCL>(tkey, qf));
+                                found = m ? __ldcg(&a.s.top_pos[(size_t)rpf * kTopEntries + 31 - __clz(m)])
+                                          : find_left<T, WT, INCL, MAPF>(qf, range_end(rpf), d_in, tile_min_r, chunk_min_r, a);
+                            }
+                        }
                         if (found < 0) {
                             if (lane == 0) atomicOr(err, ERR_INTERNAL);
                             pend = 0;
@@ -1473,6 +1542,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         }
                     }
                 }
+              }
             }
         }
 
@@ -1489,12 +1559,17 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         }
         if (cap_total > kCapCap) {
             // B'. the capped list overflowed: every flagged key of the mixed tiles after it
+            //     (flag and mask words loaded 32 at a time, as in A')
             const int from = sCapP[kCapCap - 1] + 1;
-            for (int t = from / WT; t < t1; t++) {
-                const uint32_t tf = __ldcg(&a.s.tile_flag[t]);
-                if ((tf >> 31) == 0) continue;
+            for (int tb = from / WT; tb < t1; tb += 32) {
+              const uint32_t tfl = tb + lane < t1 ? __ldcg(&a.s.tile_flag[tb + lane]) : 0u;
+              unsigned fl = __ballot_sync(FULL, (tfl >> 31) != 0);
+              while (fl) {
+                const int t = tb + __ffs(fl) - 1;
+                fl &= fl - 1;
+                const uint32_t mwl = lane < W ? __ldcg(&a.s.tile_mask[(size_t)t * MW + lane]) : 0u;
                 for (int w = 0; w < W; w++) {
-                    const uint32_t mw = __ldcg(&a.s.tile_mask[(size_t)t * MW + w]);
+                    const uint32_t mw = __shfl_sync(FULL, mwl, w);
                     const int pos = t * WT + w * 32 + lane;
                     unsigned pend = __ballot_sync(FULL, ((mw >> lane) & 1u) && pos >= from && (!head || pos >= head));
                     while (pend) {
@@ -1511,6 +1586,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         }
                     }
                 }
+              }
             }
         }
     }
