@@ -5,8 +5,9 @@ The engine has one tunable knob, the kernel configuration: warps per CTA
 lane would double the in-lane compare ladder's cost per key, and there is no
 cluster dimension: ranges are warp-independent).  A size class is floor(log2(n)); the tuner
 times every configuration on seeded synthetic arrays of that size (uniform,
-descending and ascending keys, the single-array benchmark's inputs), keeps the
-one with the lowest total time, and stores {class: config} in a table.  A
+descending and ascending keys, the single-array benchmark's inputs; the runs
+replayed from a CUDA graph, so device time without host enqueue cost), keeps
+the one with the lowest total time, and stores {class: config} in a table.  A
 Plan (or apse / the server) given a table picks the configuration per call:
 
     table = autotune.tune(dtype=torch.int32, classes=range(14, 27))
@@ -120,16 +121,27 @@ def tune(dtype: torch.dtype = torch.int32, classes=range(14, 27), reps: int = 5,
             per = {}
             for cfg in range(num_configs()):
                 plan.set_config(cfg)
-                for x in xs:  # warm-up
-                    plan.run(x, out=out[:n])
+                # the runs replayed from a CUDA graph: device time, without the
+                # host's enqueue cost (which alone exceeds a small array's run)
+                side = torch.cuda.Stream(device=dev)
+                side.wait_stream(torch.cuda.current_stream(dev))
+                with torch.cuda.stream(side):
+                    for x in xs:  # warm-up (first launches set kernel attributes)
+                        plan.run(x, out=out[:n])
+                torch.cuda.synchronize(dev)
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph, stream=side):
+                    for _ in range(reps):
+                        for x in xs:
+                            plan.run(x, out=out[:n])
+                graph.replay()
                 torch.cuda.synchronize(dev)
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record()
-                for _ in range(reps):
-                    for x in xs:
-                        plan.run(x, out=out[:n])
+                graph.replay()
                 e1.record()
                 plan.check()
+                del graph
                 t = e0.elapsed_time(e1)
                 per[cfg] = t * 1e3 / (reps * len(xs))
                 if verbose:

@@ -10,10 +10,14 @@
 //   largest rectangle = max over i of h[i] * (next smaller - previous smaller - 1)
 //   Cartesian parent  = of previous smaller-or-equal and next smaller, the one
 //                       with the larger key (ties: the next one)
-// Each is a few memory-bound passes (flip / reverse / mirror / epilogue,
-// grid-stride, coalesced) around one or two engine runs on the caller's plan
-// and stream, with a caller-provided workspace: no allocation, no
-// synchronisation, graph-capturable like apsep_run.
+// Previous greater and the stock span are one engine run each with the keys
+// flipped as they load (and, for the span, position - answer as the answers
+// leave: apsep_mapped.cu) when the keys are 4 bytes on a 16-byte boundary;
+// the rest, and those otherwise, are a few memory-bound passes (flip /
+// reverse / mirror / epilogue, grid-stride, coalesced) around one or two
+// engine runs on the caller's plan and stream, with a caller-provided
+// workspace: no allocation, no synchronisation, graph-capturable like
+// apsep_run.
 #include <stdint.h>
 
 #include <type_traits>
@@ -173,6 +177,9 @@ apsep_status apsep_run_prev_greater(apsep_plan* plan, const void* d_in, int32_t*
     int dtype = 0;
     apsep_status s = check_args(plan, d_in, d_out, (size_t)n * 4, n, d_work, &dtype);
     if (s != APSEP_OK || n == 0) return s;
+    // one engine run that flips the keys as it loads them (4-byte keys on a
+    // 16-byte boundary), else a flip pass into the workspace and a plain run
+    if ((s = plan_run_flipped(plan, d_in, d_out, n, cmp, 0, stream)) != APSEP_ENOTSUP) return s;
     const cudaStream_t st = (cudaStream_t)stream;
     for_key_type(dtype, [&](auto tag) {
         using T = std::remove_pointer_t<decltype(tag)>;
@@ -201,7 +208,13 @@ apsep_status apsep_run_next_smaller(apsep_plan* plan, const void* d_in, int32_t*
 
 apsep_status apsep_stock_span(apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, void* d_work,
                               void* stream) {
-    apsep_status s = apsep_run_prev_greater(plan, d_in, d_out, n, APSEP_LT, d_work, stream);
+    int dtype = 0;
+    apsep_status s = check_args(plan, d_in, d_out, (size_t)n * 4, n, d_work, &dtype);
+    if (s != APSEP_OK || n == 0) return s;
+    // one engine run that flips the keys as it loads them and writes
+    // position - answer, when it has that form for the call
+    if ((s = plan_run_flipped(plan, d_in, d_out, n, APSEP_LT, 1, stream)) != APSEP_ENOTSUP) return s;
+    s = apsep_run_prev_greater(plan, d_in, d_out, n, APSEP_LT, d_work, stream);
     if (s != APSEP_OK || n == 0) return s;
     span_from_previous<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(d_out, n);
     return launched();

@@ -62,11 +62,25 @@ template <> struct KeyTraits<int64_t> {
 __device__ __forceinline__ int64_t f64_order(int64_t b) {
     return (b << 1) == 0 ? 0 : (b ^ ((b >> 63) & 0x7fffffffffffffffLL));
 }
-// A key from global memory, mapped when MAPF (int64 slots holding float64 bits).
-template <typename T, bool MAPF>
+// Key maps, applied as keys enter registers or shared memory (the engine's
+// KMAP template parameter): KMAP_F64 -- int64 slots holding float64 bit
+// patterns, compared through f64_order; KMAP_FLIP -- the order-reversing map
+// (integers ~x = -x - 1, floats -x; the two zeros stay equal), so that a
+// previous-smaller run answers previous-greater queries.
+constexpr int KMAP_NONE = 0, KMAP_F64 = 1, KMAP_FLIP = 2;
+__device__ __forceinline__ int32_t flip_key(int32_t x) { return ~x; }
+__device__ __forceinline__ float flip_key(float x) { return -x; }
+__device__ __forceinline__ int64_t flip_key(int64_t x) { return ~x; }
+template <typename T, int KMAP>
+__device__ __forceinline__ T map_key(T x) {
+    if constexpr (KMAP == KMAP_F64) return (T)f64_order((int64_t)x);
+    else if constexpr (KMAP == KMAP_FLIP) return flip_key(x);
+    else return x;
+}
+// A key from global memory, through the key map.
+template <typename T, int KMAP>
 __device__ __forceinline__ T load_key(const T* p) {
-    if constexpr (MAPF) return (T)f64_order((int64_t)__ldg(p));
-    else return __ldg(p);
+    return map_key<T, KMAP>(__ldg(p));
 }
 
 // lt(a, b): "a qualifies as the answer for query b".  INCL=false is the

@@ -121,6 +121,9 @@ struct RangeArgs {
 // their range is not written at all; its tile_flag word carries
 // TILE_NOT_STORED (phase 2 still writes the keys that it answers).
 constexpr int64_t UNRESOLVED64 = -2;
+// Output forms of a run (the engine's OUTM template parameter): int32
+// answers; int64 answers (above); int32 spans, position - answer.
+constexpr int OUT_I32 = 0, OUT_I64 = 1, OUT_SPAN = 2;
 constexpr uint32_t TILE_NOT_STORED = 0x40000000u;
 
 // The TMA view of a run: the number of virtual keys (0..3) in front of d_in
@@ -168,6 +171,11 @@ cudaError_t range_max_warps(int cfg, int* warps);  // persistent warps of one la
 // a.d_out64 (4-byte keys in configuration 0, 8-byte keys in theirs); flagged keys
 // get UNRESOLVED64 and all-deferred tiles are not written (TILE_NOT_STORED).
 cudaError_t launch_range_out64(int dtype, int incl, RangeArgs& a, const CUtensorMap& map_in, cudaStream_t st);
+// A single array (no view head, 4-byte keys) through the order-reversing key
+// map in configuration 0: previous-greater answers (int32), or with span != 0
+// (strict comparison only) the stock span, position - answer.
+cudaError_t launch_range_flipped(int dtype, int incl, int span, RangeArgs& a, const CUtensorMap& map_in,
+                                 const CUtensorMap& map_out, cudaStream_t st);
 // Arms one-shot fault injection for the next apsep_run_noalloc call.
 void noalloc_debug_inject(int32_t range, uint32_t spin_limit);
 
@@ -180,5 +188,12 @@ struct apsep_plan;
 // chunk_min, when not null, takes the run's minima of every 32 keys (in key
 // order, up to the end of the last tile) instead of the plan's scratch.
 // *layout returns the run's arguments: tile and range layout, scratch words.
+// One single-array run of the plan through the order-reversing key map
+// (launch_range_flipped): previous greater (span = 0) or the stock span
+// (span = 1, APSEP_LT).  APSEP_ENOTSUP when the engine has no such form for
+// the call (8-byte keys, or keys and answers at different 16-byte phases):
+// the caller then takes its general route.
+apsep_status plan_run_flipped(struct apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                              int span, void* stream);
 apsep_status plan_run_out64(struct apsep_plan* plan, const void* d_in, int64_t* d_out, int64_t n, int64_t out_base,
                             apsep_cmp cmp, void* chunk_min, void* stream, apsep::RangeArgs* layout);

@@ -14,10 +14,10 @@ namespace {
 constexpr int kMaxDevO = 64;
 int g_warps64[kMaxDevO][2];  // resident warps per device: [0] 4-byte keys, [1] 8-byte keys
 
-template <typename T, int IPT, int WPC, bool MAPF>
+template <typename T, int IPT, int WPC, int KMAP>
 cudaError_t prep(int* per_sm) {
-    cudaError_t rr[2] = {prepare_t<T, IPT, WPC, false, false, true, MAPF, true>(per_sm),
-                         prepare_t<T, IPT, WPC, true, false, true, MAPF, true>(per_sm)};
+    cudaError_t rr[2] = {prepare_t<T, IPT, WPC, false, false, true, KMAP, OUT_I64>(per_sm),
+                         prepare_t<T, IPT, WPC, true, false, true, KMAP, OUT_I64>(per_sm)};
     return rr[0] != cudaSuccess ? rr[0] : rr[1];
 }
 
@@ -29,11 +29,11 @@ cudaError_t warps_for(int wide, int* warps) {
     if (!g_warps64[dev][wide]) {
         int per_sm = 0;
         if (wide) {
-            if ((e = prep<int64_t, 8, 8, false>(&per_sm)) != cudaSuccess) return e;
-            if ((e = prep<int64_t, 8, 8, true>(&per_sm)) != cudaSuccess) return e;
+            if ((e = prep<int64_t, 8, 8, KMAP_NONE>(&per_sm)) != cudaSuccess) return e;
+            if ((e = prep<int64_t, 8, 8, KMAP_F64>(&per_sm)) != cudaSuccess) return e;
         } else {
-            if ((e = prep<int32_t, 16, 16, false>(&per_sm)) != cudaSuccess) return e;
-            if ((e = prep<float, 16, 16, false>(&per_sm)) != cudaSuccess) return e;
+            if ((e = prep<int32_t, 16, 16, KMAP_NONE>(&per_sm)) != cudaSuccess) return e;
+            if ((e = prep<float, 16, 16, KMAP_NONE>(&per_sm)) != cudaSuccess) return e;
         }
         int sms = 0;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
@@ -57,17 +57,17 @@ cudaError_t launch_range_out64(int dtype, int incl, RangeArgs& a, const CUtensor
     const CUtensorMap& mo = mi;  // (no tensor store: answers leave as int64 from registers)
     switch (dtype) {
     case 0:
-        return incl ? launch_t<int32_t, 16, 16, true, false, true, false, true>(a, mi, mo, st, max_warps)
-                    : launch_t<int32_t, 16, 16, false, false, true, false, true>(a, mi, mo, st, max_warps);
+        return incl ? launch_t<int32_t, 16, 16, true, false, true, KMAP_NONE, OUT_I64>(a, mi, mo, st, max_warps)
+                    : launch_t<int32_t, 16, 16, false, false, true, KMAP_NONE, OUT_I64>(a, mi, mo, st, max_warps);
     case 1:
-        return incl ? launch_t<float, 16, 16, true, false, true, false, true>(a, mi, mo, st, max_warps)
-                    : launch_t<float, 16, 16, false, false, true, false, true>(a, mi, mo, st, max_warps);
+        return incl ? launch_t<float, 16, 16, true, false, true, KMAP_NONE, OUT_I64>(a, mi, mo, st, max_warps)
+                    : launch_t<float, 16, 16, false, false, true, KMAP_NONE, OUT_I64>(a, mi, mo, st, max_warps);
     case 2:
-        return incl ? launch_t<int64_t, 8, 8, true, false, true, false, true>(a, mi, mo, st, max_warps)
-                    : launch_t<int64_t, 8, 8, false, false, true, false, true>(a, mi, mo, st, max_warps);
+        return incl ? launch_t<int64_t, 8, 8, true, false, true, KMAP_NONE, OUT_I64>(a, mi, mo, st, max_warps)
+                    : launch_t<int64_t, 8, 8, false, false, true, KMAP_NONE, OUT_I64>(a, mi, mo, st, max_warps);
     default:  // float64 keys compare as their order-preserving int64 map
-        return incl ? launch_t<int64_t, 8, 8, true, false, true, true, true>(a, mi, mo, st, max_warps)
-                    : launch_t<int64_t, 8, 8, false, false, true, true, true>(a, mi, mo, st, max_warps);
+        return incl ? launch_t<int64_t, 8, 8, true, false, true, KMAP_F64, OUT_I64>(a, mi, mo, st, max_warps)
+                    : launch_t<int64_t, 8, 8, false, false, true, KMAP_F64, OUT_I64>(a, mi, mo, st, max_warps);
     }
 }
 

@@ -172,7 +172,7 @@ static __device__ __noinline__ int seg_find(const int64_t* __restrict__ off, int
 // Answer relative to the segment start s: an answer before the segment is none.
 __device__ __forceinline__ int seg_rel(int g, int s) { return g >= s ? g - s : -1; }
 
-template <typename T, int B, bool INCL, bool MAPF = false>
+template <typename T, int B, bool INCL, int MAPF = KMAP_NONE>
 __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in, const T* __restrict__ tile_min,
                                       const T* __restrict__ chunk_min, const RangeArgs& a) {
     constexpr int W = B / 32;
@@ -387,15 +387,17 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
     }
 }
 
-// MAPF: int64 key slots that hold float64 bit patterns, compared through
-// f64_order (keys are mapped as they enter shared memory or registers).
-// OUT64 (single arrays, no view head): answers as int64, a.out_base + answer,
-// into a.d_out64, for the int64-position path: a flagged key gets UNRESOLVED64
-// (phase 2 overwrites the ones it answers), and a tile whose keys are all
-// deferred is not written at all (its flag word says so); the int64-position
-// path answers what is left.
+// MAPF: the key map (KMAP_*): keys pass through it as they enter shared memory
+// or registers -- float64 bit patterns in int64 slots compared through
+// f64_order, or the order-reversing flip for previous-greater queries.
+// OUTM (single arrays, no view head, except OUT_I32): OUT_I64 -- answers as
+// int64, a.out_base + answer, into a.d_out64, for the int64-position path: a
+// flagged key gets UNRESOLVED64 (phase 2 overwrites the ones it answers), and a
+// tile whose keys are all deferred is not written at all (its flag word says
+// so); the int64-position path answers what is left.  OUT_SPAN -- int32
+// position - answer (position + 1 for none): the stock span, with the flip.
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false, bool OUT64 = false>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32>
 __global__ void __launch_bounds__(WPC * 32, (WPC >= 16 && sizeof(T) == 4 ? 1 : 2))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
@@ -446,11 +448,14 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         return a.offsets ? (int64_t)__ldg(&a.offsets[i]) : (i == 0 ? (int64_t)0 : (int64_t)(a.n - head));
     };
     auto seg_idx = [&](int pos) { return a.offsets ? seg_find(a.offsets, a.nseg, pos, err) : 0; };
-    static_assert(!OUT64 || (!SEG && EP), "int64 answers: single arrays only");
+    static_assert(OUTM == OUT_I32 || (!SEG && EP), "int64 and span answers: single arrays only");
+    constexpr bool OUT64 = OUTM == OUT_I64;
     // a final answer v of position pos (phase 2); int64 answers: out_base + v, and
-    // UNRESOLVED64 for none (the key is left to the int64-position path)
+    // UNRESOLVED64 for none (the key is left to the int64-position path); spans:
+    // pos - v
     auto put = [&](int pos, int v) {
         if constexpr (OUT64) a.d_out64[pos] = v >= 0 ? (int64_t)v + a.out_base : UNRESOLVED64;
+        else if constexpr (OUTM == OUT_SPAN) a.d_out[pos] = pos - v;
         else a.d_out[pos] = v;
     };
 
@@ -520,11 +525,11 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 
             if (full) {
                 if (!mbar_wait_bounded(&bar[slot], par, a.spin_limit) && lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
-                if constexpr (MAPF) {  // the tile's float64 bits become ordered int64 keys, in place
+                if constexpr (MAPF != KMAP_NONE) {  // the tile's keys through the key map, in place
 #pragma unroll
                     for (int j = 0; j < IPT; j++) {
                         const int e = j * 32 + lane;
-                        V[ks(e)] = (T)f64_order((int64_t)V[ks(e)]);
+                        V[ks(e)] = map_key<T, MAPF>(V[ks(e)]);
                     }
                 }
             } else {
@@ -532,7 +537,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 for (int j = 0; j < IPT; j++) {
                     const int e = j * 32 + lane;
                     const int g = tile_base + e;
-                    V[ks(e)] = g < a.n && (!head || g >= head) ? (MAPF ? load_key<T, MAPF>(&d_in[g]) : d_in[g])
+                    V[ks(e)] = g < a.n && (!head || g >= head) ? (MAPF != KMAP_NONE ? load_key<T, MAPF>(&d_in[g]) : d_in[g])
                                                                 : KeyTraits<T>::pad();
                 }
                 // A view head makes tile 0 plain while tile kStages streams into its
@@ -670,6 +675,20 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     }
                     return;
                 }
+                if constexpr (OUTM == OUT_SPAN) {  // spans: position - answer
+                    __syncwarp();                   // every lane's answers are in O
+    #pragma unroll
+                    for (int q4 = 0; q4 < IPT / 4; q4++) {
+                        int4* po = reinterpret_cast<int4*>(&O[swz(lane * IPT + 4 * q4)]);
+                        int4 o = *po;
+                        const int p0 = tile_base + lane * IPT + 4 * q4;
+                        o.x = p0 - o.x;
+                        o.y = p0 + 1 - o.y;
+                        o.z = p0 + 2 - o.z;
+                        o.w = p0 + 3 - o.w;
+                        *po = o;
+                    }
+                }
                 if constexpr (SEG) {  // answers relative to their segment's start
                     __syncwarp();     // every lane's answers are in O
     #pragma unroll
@@ -755,7 +774,9 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         __stcg(&tile_min_w[t], tmin);
                     }
                     def_total += WT;
-                    if constexpr (!OUT64) {  // (int64 answers: the tile is left to the int64-position path)
+                    if constexpr (OUTM == OUT_SPAN) {
+                        store_tile();
+                    } else if constexpr (!OUT64) {  // (int64 answers: the tile is left to the int64-position path)
                         fence_proxy_async_smem();
                         __syncwarp();
                         if (full) {
@@ -819,7 +840,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         __stcg(&a.s.tile_flag[t], 0u);
                         __stcg(&tile_min_w[t], first);
                     }
-                    if constexpr (OUT64) {
+                    if constexpr (OUTM != OUT_I32) {
                         store_tile();
                     } else {
                         fence_proxy_async_smem();
@@ -1617,7 +1638,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 // ---------------------------------------------------------------------------
 // Launch plumbing shared by the single-array and segmented translation units.
 // ---------------------------------------------------------------------------
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false, bool OUT64 = false>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32>
 inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo, cudaStream_t st,
                             int max_warps) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
@@ -1626,14 +1647,14 @@ inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorM
     a.tiles_per_range = tpr;
     a.num_ranges = (a.num_tiles + tpr - 1) / tpr;
     const int ctas = (a.num_ranges + WPC - 1) / WPC;
-    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUT64><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
+    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUTM><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
     return cudaGetLastError();
 }
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, bool MAPF = false, bool OUT64 = false>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32>
 inline cudaError_t prepare_t(int* ctas_per_sm) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
-    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUT64>;
+    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUTM>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int n = 0;

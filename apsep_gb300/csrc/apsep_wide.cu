@@ -30,12 +30,12 @@ cudaError_t prepare_wide() {
     int per_sm = 0;
     cudaError_t rr[8] = {prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true>(&per_sm),
                          prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true>(&per_sm),
-                         prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true, true>(&per_sm),
-                         prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true, true>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, false, false, true, KMAP_F64>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, true, false, true, KMAP_F64>(&per_sm),
                          prepare_t<int64_t, kWideIpt, kWideWpc, false, true, false>(&per_sm),
                          prepare_t<int64_t, kWideIpt, kWideWpc, true, true, false>(&per_sm),
-                         prepare_t<int64_t, kWideIpt, kWideWpc, false, true, false, true>(&per_sm),
-                         prepare_t<int64_t, kWideIpt, kWideWpc, true, true, false, true>(&per_sm)};
+                         prepare_t<int64_t, kWideIpt, kWideWpc, false, true, false, KMAP_F64>(&per_sm),
+                         prepare_t<int64_t, kWideIpt, kWideWpc, true, true, false, KMAP_F64>(&per_sm)};
     for (int q = 0; q < 8; q++)
         if (rr[q] != cudaSuccess) return rr[q];
     int sms = 0;
@@ -61,16 +61,16 @@ cudaError_t launch_range_wide(int dtype, int incl, RangeArgs& a, const CUtensorM
         if (dtype == 2)
             return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, true, false>(a, mi, mo, st, max_warps)
                         : launch_t<int64_t, kWideIpt, kWideWpc, false, true, false>(a, mi, mo, st, max_warps);
-        return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, true, false, true>(a, mi, mo, st, max_warps)
-                    : launch_t<int64_t, kWideIpt, kWideWpc, false, true, false, true>(a, mi, mo, st, max_warps);
+        return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, true, false, KMAP_F64>(a, mi, mo, st, max_warps)
+                    : launch_t<int64_t, kWideIpt, kWideWpc, false, true, false, KMAP_F64>(a, mi, mo, st, max_warps);
     }
     a.nseg = 0;
     if (dtype == 2)
         return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, false, true>(a, mi, mo, st, max_warps)
                     : launch_t<int64_t, kWideIpt, kWideWpc, false, false, true>(a, mi, mo, st, max_warps);
     // float64: int64 slots compared through the order map (no FP64 compares)
-    return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, false, true, true>(a, mi, mo, st, max_warps)
-                : launch_t<int64_t, kWideIpt, kWideWpc, false, false, true, true>(a, mi, mo, st, max_warps);
+    return incl ? launch_t<int64_t, kWideIpt, kWideWpc, true, false, true, KMAP_F64>(a, mi, mo, st, max_warps)
+                : launch_t<int64_t, kWideIpt, kWideWpc, false, false, true, KMAP_F64>(a, mi, mo, st, max_warps);
 }
 
 }  // namespace apsep

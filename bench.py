@@ -341,9 +341,9 @@ def run_consumers(dev, peak_gbs: float) -> dict:
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ops = {  # name: (call, caller bytes per key, pass bytes per key)
-        "prev_greater": (lambda: consumers.prev_greater(x, plan=plan, work=work), 8, 16),
+        "prev_greater": (lambda: consumers.prev_greater(x, plan=plan, work=work), 8, 8),  # one flipped run
         "next_smaller": (lambda: consumers.next_smaller(x, plan=plan, work=work), 8, 24),
-        "stock_span": (lambda: consumers.stock_span(x, plan=plan, work=work), 8, 24),
+        "stock_span": (lambda: consumers.stock_span(x, plan=plan, work=work), 8, 8),  # flipped run, span out
         "cartesian_parents": (lambda: consumers.cartesian_parents(x, plan=plan, work=work), 8, 40),
         "largest_rectangle": (lambda: consumers.largest_rectangle(h, plan=plan, work=work), 4, 36),
     }

@@ -122,3 +122,32 @@ def test_invalid_arguments(plans):
     assert int(area.item()) == 0
     with pytest.raises(ValueError):
         consumers.prev_greater(x.cpu())
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.float32])
+@pytest.mark.parametrize("shift", [0, 1, 3])
+def test_flipped_run_and_its_general_route(plans, dtype, shift):
+    # keys (and answers) on a 16-byte boundary take the one-run form (keys
+    # flipped as they load, spans written as they leave); one or three keys
+    # past it, the flip pass and a plain run: both bit-exact, with the
+    # extreme keys the flip maps onto the engine's pad value
+    rng = np.random.default_rng(40 + shift)
+    plan = plans[dtype]
+    n = 300_007
+    for name in ("uniform", "dup16", "desc", "asc"):
+        a = keys(name, n, rng, dtype)
+        if dtype == np.int32:
+            a[rng.integers(0, n, 200)] = np.iinfo(np.int32).min
+            a[rng.integers(0, n, 200)] = np.iinfo(np.int32).max
+        else:
+            a[rng.integers(0, n, 200)] = -np.inf
+            a[rng.integers(0, n, 200)] = np.float32(-0.0)
+            a[rng.integers(0, n, 200)] = np.float32(0.0)
+        base = torch.zeros(n + shift, dtype=torch.from_numpy(a[:0]).dtype, device="cuda")
+        base[shift:] = torch.from_numpy(a).cuda()
+        x = base[shift:]
+        for le in (False, True):
+            check(consumers.prev_greater(x, le, plan=plan).cpu().numpy(), oc.prev_greater(a, le),
+                  "prev_greater %s %s" % (name, le))
+        check(consumers.stock_span(x, plan=plan).cpu().numpy(), oc.stock_span(a), "stock_span %s" % name)
+    plan.check()
