@@ -337,6 +337,43 @@ apsep_status plan_run_flipped(apsep_plan* p, const void* d_in, int32_t* d_out, i
     return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
 }
 
+apsep_status plan_run_reversed(apsep_plan* p, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                               void* stream) {
+    if (!p || n <= 0 || n > p->capacity || !d_in || !d_out || (cmp != APSEP_LT && cmp != APSEP_LE)) return APSEP_EINVAL;
+    if (wide(p->dtype) || n % 32 != 0) return APSEP_ENOTSUP;
+    if ((uintptr_t)d_in % 16 != 0 || (uintptr_t)d_out % 16 != 0) return APSEP_ENOTSUP;
+    if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_EINVAL;
+    DeviceGuard g(p->device);
+    if (!g.ok) return APSEP_ECUDA;
+    const int B = 32 * kTileConfigs[0].ipt;  // keys per warp tile
+    const int tile_rows = B / 32;
+    int rows = (int)(n / 32);
+    CUtensorMap mi, mo;
+    memset(&mi, 0, sizeof(mi));
+    memset(&mo, 0, sizeof(mo));
+    if (rows < tile_rows) rows = 0;
+    if (rows > 0 && (!encode_rows(&mi, d_in, rows, tile_rows, p->dtype) || !encode_rows(&mo, d_out, rows, tile_rows, 0)))
+        return APSEP_ECUDA;
+    RangeArgs a;
+    a.d_in = d_in;
+    a.d_out = d_out;
+    a.n = (int)n;
+    a.head = 0;
+    a.num_tiles = (int)((n + B - 1) / B);
+    a.tiles_per_range = 0;
+    a.num_ranges = 0;
+    a.tma_rows = rows;
+    a.spin_limit = p->dbg_spin_limit ? p->dbg_spin_limit : kDefaultSpinLimit;
+    a.skip_publish_range = p->dbg_skip_range;
+    a.offsets = nullptr;
+    a.nseg = 1;
+    a.s = p->rs;
+    p->dbg_skip_range = -1;
+    p->dbg_spin_limit = 0;
+    const cudaError_t e = launch_range_reversed(p->dtype, cmp == APSEP_LE ? 1 : 0, a, mi, mo, (cudaStream_t)stream);
+    return e == cudaSuccess ? APSEP_OK : APSEP_ECUDA;
+}
+
 apsep_status plan_run_out64(apsep_plan* p, const void* d_in, int64_t* d_out, int64_t n, int64_t out_base,
                             apsep_cmp cmp, void* chunk_min, void* stream, RangeArgs* layout) {
     if (!p || !layout || n <= 0 || n > p->capacity || !d_in || !d_out || (cmp != APSEP_LT && cmp != APSEP_LE))

@@ -10,14 +10,16 @@
 //   largest rectangle = max over i of h[i] * (next smaller - previous smaller - 1)
 //   Cartesian parent  = of previous smaller-or-equal and next smaller, the one
 //                       with the larger key (ties: the next one)
-// Previous greater and the stock span are one engine run each with the keys
-// flipped as they load (and, for the span, position - answer as the answers
-// leave: apsep_mapped.cu) when the keys are 4 bytes on a 16-byte boundary;
-// the rest, and those otherwise, are a few memory-bound passes (flip /
-// reverse / mirror / epilogue, grid-stride, coalesced) around one or two
-// engine runs on the caller's plan and stream, with a caller-provided
-// workspace: no allocation, no synchronisation, graph-capturable like
-// apsep_run.
+// With 4-byte keys on a 16-byte boundary the engine does the flips and
+// reversals itself (apsep_mapped.cu): previous greater and the stock span are
+// one run each with the keys flipped as they load (and position - answer as
+// the answers leave), next smaller one run over the reversed array with its
+// answers mirrored as they leave (n a multiple of 32), and the histogram and
+// Cartesian tree take that run for their next-smaller half.  Otherwise each is
+// a few memory-bound passes (flip / reverse / mirror / epilogue, grid-stride,
+// coalesced) around one or two engine runs.  All run on the caller's plan and
+// stream with a caller-provided workspace: no allocation, no synchronisation,
+// graph-capturable like apsep_run.
 #include <stdint.h>
 
 #include <type_traits>
@@ -85,6 +87,11 @@ __device__ __forceinline__ int64_t next_from_reversed(const int32_t* __restrict_
     const int32_t a = ar[n - 1 - i];
     return a >= 0 ? n - 1 - a : -1;
 }
+// next[i] from R: the next-smaller answers themselves (direct, a reversed run
+// of the engine), or the reversed array's previous-smaller answers.
+__device__ __forceinline__ int64_t next_of(const int32_t* __restrict__ R, bool direct, int64_t n, int64_t i) {
+    return direct ? (int64_t)R[i] : next_from_reversed(R, n, i);
+}
 
 __global__ void mirror_answers(const int32_t* __restrict__ ar, int32_t* __restrict__ out, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -100,11 +107,11 @@ __global__ void span_from_previous(int32_t* __restrict__ a, int64_t n) {
 // next strictly smaller (n: none).  Only positive areas compete (heights are
 // non-negative by contract; a negative height contributes nothing).
 __global__ void rect_area(const int32_t* __restrict__ h, const int32_t* __restrict__ L,
-                          const int32_t* __restrict__ ar, int64_t n, unsigned long long* __restrict__ best) {
+                          const int32_t* __restrict__ ar, bool direct, int64_t n, unsigned long long* __restrict__ best) {
     __shared__ long long warp_best[kThreads / 32];
     long long m = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = next_from_reversed(ar, n, i);
+        const int64_t r = next_of(ar, direct, n, i);
         const int64_t w = (r < 0 ? n : r) - (int64_t)L[i] - 1;
         const long long area = (long long)h[i] * w;
         m = area > m ? area : m;
@@ -128,9 +135,9 @@ __global__ void rect_area(const int32_t* __restrict__ h, const int32_t* __restri
 // larger key, R on a tie; -1 for the root.
 template <typename T>
 __global__ void cartesian_parent(const T* __restrict__ a, const int32_t* __restrict__ L,
-                                 const int32_t* __restrict__ ar, int32_t* __restrict__ out, int64_t n) {
+                                 const int32_t* __restrict__ ar, bool direct, int32_t* __restrict__ out, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t l = L[i], r = next_from_reversed(ar, n, i);
+        const int64_t l = L[i], r = next_of(ar, direct, n, i);
         int64_t p;
         if (r < 0) p = l;
         else if (l < 0) p = r;
@@ -194,6 +201,9 @@ apsep_status apsep_run_next_smaller(apsep_plan* plan, const void* d_in, int32_t*
     int dtype = 0;
     apsep_status s = check_args(plan, d_in, d_out, (size_t)n * 4, n, d_work, &dtype);
     if (s != APSEP_OK || n == 0) return s;
+    // one engine run over the reversed array, answers mirrored as they leave,
+    // when it has that form for the call; else reverse, run, mirror
+    if ((s = plan_run_reversed(plan, d_in, d_out, n, cmp, stream)) != APSEP_ENOTSUP) return s;
     const cudaStream_t st = (cudaStream_t)stream;
     const Work w = carve(d_work, n, dtype);
     for_key_type(dtype, [&](auto tag) {
@@ -232,10 +242,17 @@ apsep_status apsep_largest_rectangle(apsep_plan* plan, const int32_t* d_heights,
     if (n == 0) return APSEP_OK;
     const Work w = carve(d_work, n, dtype);
     if ((s = apsep_run_cmp(plan, d_heights, w.b, n, APSEP_LT, stream)) != APSEP_OK) return s;
-    reverse_keys<int32_t><<<grid_for(n), kThreads, 0, st>>>(d_heights, (int32_t*)w.keys, n);
-    if ((s = launched()) != APSEP_OK) return s;
-    if ((s = apsep_run_cmp(plan, w.keys, w.a, n, APSEP_LT, stream)) != APSEP_OK) return s;
-    rect_area<<<grid_for(n), kThreads, 0, st>>>(d_heights, w.b, w.a, n, (unsigned long long*)d_area);
+    // next smaller: one reversed run when the engine has that form, else
+    // reverse the heights and run (the answers then come mirrored)
+    bool direct = true;
+    if ((s = plan_run_reversed(plan, d_heights, w.a, n, APSEP_LT, stream)) == APSEP_ENOTSUP) {
+        direct = false;
+        reverse_keys<int32_t><<<grid_for(n), kThreads, 0, st>>>(d_heights, (int32_t*)w.keys, n);
+        if ((s = launched()) != APSEP_OK) return s;
+        s = apsep_run_cmp(plan, w.keys, w.a, n, APSEP_LT, stream);
+    }
+    if (s != APSEP_OK) return s;
+    rect_area<<<grid_for(n), kThreads, 0, st>>>(d_heights, w.b, w.a, direct, n, (unsigned long long*)d_area);
     return launched();
 }
 
@@ -247,15 +264,20 @@ apsep_status apsep_cartesian_parents(apsep_plan* plan, const void* d_in, int32_t
     const cudaStream_t st = (cudaStream_t)stream;
     const Work w = carve(d_work, n, dtype);
     if ((s = apsep_run_cmp(plan, d_in, w.b, n, APSEP_LE, stream)) != APSEP_OK) return s;
+    bool direct = true;  // next smaller straight from a reversed run, else mirrored
+    if ((s = plan_run_reversed(plan, d_in, w.a, n, APSEP_LT, stream)) == APSEP_ENOTSUP) {
+        direct = false;
+        for_key_type(dtype, [&](auto tag) {
+            using T = std::remove_pointer_t<decltype(tag)>;
+            reverse_keys<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, (T*)w.keys, n);
+        });
+        if ((s = launched()) != APSEP_OK) return s;
+        s = apsep_run_cmp(plan, w.keys, w.a, n, APSEP_LT, stream);
+    }
+    if (s != APSEP_OK) return s;
     for_key_type(dtype, [&](auto tag) {
         using T = std::remove_pointer_t<decltype(tag)>;
-        reverse_keys<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, (T*)w.keys, n);
-    });
-    if ((s = launched()) != APSEP_OK) return s;
-    if ((s = apsep_run_cmp(plan, w.keys, w.a, n, APSEP_LT, stream)) != APSEP_OK) return s;
-    for_key_type(dtype, [&](auto tag) {
-        using T = std::remove_pointer_t<decltype(tag)>;
-        cartesian_parent<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, w.b, w.a, d_out, n);
+        cartesian_parent<T><<<grid_for(n), kThreads, 0, st>>>((const T*)d_in, w.b, w.a, direct, d_out, n);
     });
     return launched();
 }

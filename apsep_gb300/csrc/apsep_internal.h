@@ -176,6 +176,11 @@ cudaError_t launch_range_out64(int dtype, int incl, RangeArgs& a, const CUtensor
 // (strict comparison only) the stock span, position - answer.
 cudaError_t launch_range_flipped(int dtype, int incl, int span, RangeArgs& a, const CUtensorMap& map_in,
                                  const CUtensorMap& map_out, cudaStream_t st);
+// A single array (no view head, 4-byte keys) seen reversed in configuration
+// 0: next-smaller answers (n - 1 - the reversed run's answer, at the mirrored
+// position), TMA tiles only when n is a multiple of 32 (a.tma_rows * 32 == n).
+cudaError_t launch_range_reversed(int dtype, int incl, RangeArgs& a, const CUtensorMap& map_in,
+                                  const CUtensorMap& map_out, cudaStream_t st);
 // Arms one-shot fault injection for the next apsep_run_noalloc call.
 void noalloc_debug_inject(int32_t range, uint32_t spin_limit);
 
@@ -195,5 +200,12 @@ struct apsep_plan;
 // the caller then takes its general route.
 apsep_status plan_run_flipped(struct apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
                               int span, void* stream);
+// One single-array run of the plan over the reversed array
+// (launch_range_reversed): out[i] = the next j > i with a[j] < a[i] (<= under
+// APSEP_LE), else -1.  APSEP_ENOTSUP when the engine has no such form for the
+// call (8-byte keys, keys or answers off a 16-byte boundary, n not a multiple
+// of 32): the caller then takes its general route.
+apsep_status plan_run_reversed(struct apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
+                               void* stream);
 apsep_status plan_run_out64(struct apsep_plan* plan, const void* d_in, int64_t* d_out, int64_t n, int64_t out_base,
                             apsep_cmp cmp, void* chunk_min, void* stream, apsep::RangeArgs* layout);

@@ -1,10 +1,13 @@
-// apsep_mapped.cu -- the range engine with the order-reversing key map, for
-// the consumers that ask for the previous greater key: keys are flipped as
-// they enter shared memory or registers (integers ~x, floats -x), so one run
-// of the previous-smaller engine over the unchanged input answers previous
-// greater (or greater-or-equal under <=), and with the span output form it
-// writes the stock span (position - previous strictly greater) directly.
-// Single arrays whose keys and answers share a 16-byte phase, 4-byte keys,
+// apsep_mapped.cu -- the range engine in the forms the consumers ask for:
+//   * the order-reversing key map: keys are flipped as they enter shared
+//     memory or registers (integers ~x, floats -x), so one run of the
+//     previous-smaller engine over the unchanged input answers previous
+//     greater (or greater-or-equal under <=), and with the span output form
+//     it writes the stock span (position - previous strictly greater);
+//   * the reversed array: tiles counted from the end and reversed as they
+//     land, answers mirrored as they leave, so one run answers next smaller
+//     (or smaller-or-equal).
+// Single arrays on a 16-byte boundary (keys and answers), 4-byte keys,
 // configuration 0 (16 warps per CTA, 512-key warp tiles).
 #include "apsep_range_kernel.cuh"
 
@@ -16,10 +19,12 @@ int g_warps_m[kMaxDevM];  // resident warps per device
 
 template <typename T>
 cudaError_t prep(int* per_sm) {
-    cudaError_t rr[3] = {prepare_t<T, 16, 16, false, false, true, KMAP_FLIP, OUT_I32>(per_sm),
+    cudaError_t rr[5] = {prepare_t<T, 16, 16, false, false, true, KMAP_FLIP, OUT_I32>(per_sm),
                          prepare_t<T, 16, 16, true, false, true, KMAP_FLIP, OUT_I32>(per_sm),
-                         prepare_t<T, 16, 16, false, false, true, KMAP_FLIP, OUT_SPAN>(per_sm)};
-    for (int q = 0; q < 3; q++)
+                         prepare_t<T, 16, 16, false, false, true, KMAP_FLIP, OUT_SPAN>(per_sm),
+                         prepare_t<T, 16, 16, false, false, true, KMAP_NONE, OUT_I32, true>(per_sm),
+                         prepare_t<T, 16, 16, true, false, true, KMAP_NONE, OUT_I32, true>(per_sm)};
+    for (int q = 0; q < 5; q++)
         if (rr[q] != cudaSuccess) return rr[q];
     return cudaSuccess;
 }
@@ -59,6 +64,22 @@ cudaError_t launch_range_flipped(int dtype, int incl, int span, RangeArgs& a, co
                     : launch_t<int32_t, 16, 16, false, false, true, KMAP_FLIP, OUT_I32>(a, mi, mo, st, max_warps);
     return incl ? launch_t<float, 16, 16, true, false, true, KMAP_FLIP, OUT_I32>(a, mi, mo, st, max_warps)
                 : launch_t<float, 16, 16, false, false, true, KMAP_FLIP, OUT_I32>(a, mi, mo, st, max_warps);
+}
+
+cudaError_t launch_range_reversed(int dtype, int incl, RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo,
+                                  cudaStream_t st) {
+    int max_warps = 0;
+    const cudaError_t e = warps_for(&max_warps);
+    if (e != cudaSuccess) return e;
+    if (a.head != 0 || dtype > 1 || (a.tma_rows > 0 && (int64_t)a.tma_rows * 32 != (int64_t)a.n))
+        return cudaErrorInvalidValue;
+    a.offsets = nullptr;
+    a.nseg = 1;
+    if (dtype == 0)
+        return incl ? launch_t<int32_t, 16, 16, true, false, true, KMAP_NONE, OUT_I32, true>(a, mi, mo, st, max_warps)
+                    : launch_t<int32_t, 16, 16, false, false, true, KMAP_NONE, OUT_I32, true>(a, mi, mo, st, max_warps);
+    return incl ? launch_t<float, 16, 16, true, false, true, KMAP_NONE, OUT_I32, true>(a, mi, mo, st, max_warps)
+                : launch_t<float, 16, 16, false, false, true, KMAP_NONE, OUT_I32, true>(a, mi, mo, st, max_warps);
 }
 
 }  // namespace apsep

@@ -172,7 +172,14 @@ static __device__ __noinline__ int seg_find(const int64_t* __restrict__ off, int
 // Answer relative to the segment start s: an answer before the segment is none.
 __device__ __forceinline__ int seg_rel(int g, int s) { return g >= s ? g - s : -1; }
 
-template <typename T, int B, bool INCL, int MAPF = KMAP_NONE>
+// The key at position pos of the run's array, through the key map; REV runs
+// see the array reversed (position pos is element n - 1 - pos).
+template <typename T, int KMAP, bool REV>
+__device__ __forceinline__ T key_at(const T* d_in, int n, int pos) {
+    return load_key<T, KMAP>(d_in + (REV ? n - 1 - pos : pos));
+}
+
+template <typename T, int B, bool INCL, int MAPF = KMAP_NONE, bool REV = false>
 __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in, const T* __restrict__ tile_min,
                                       const T* __restrict__ chunk_min, const RangeArgs& a) {
     constexpr int W = B / 32;
@@ -185,7 +192,7 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
     {  // 1. the row holding limit-1, positions below limit
         const int row = t * B + c * 32;
         const int p = row + lane;
-        const bool ok = p < limit && p >= a.head && lt<INCL>(load_key<T, MAPF>(&d_in[p]), q);
+        const bool ok = p < limit && p >= a.head && lt<INCL>(key_at<T, MAPF, REV>(d_in, a.n, p), q);
         const unsigned m = __ballot_sync(0xffffffffu, ok);
         if (m) return row + 31 - __clz(m);
     }
@@ -221,7 +228,7 @@ __device__ __noinline__ int find_left(T q, int limit, const T* __restrict__ d_in
     }
     const int row = s * B + cc * 32;
     const unsigned m =
-        __ballot_sync(0xffffffffu, row + lane >= a.head && lt<INCL>(load_key<T, MAPF>(&d_in[row + lane]), q));
+        __ballot_sync(0xffffffffu, row + lane >= a.head && lt<INCL>(key_at<T, MAPF, REV>(d_in, a.n, row + lane), q));
     return m ? row + 31 - __clz(m) : -2;
 }
 
@@ -396,8 +403,14 @@ __device__ void range_prefix(int r, uint32_t epoch, const RangeArgs& a, T& p, bo
 // tile whose keys are all deferred is not written at all (its flag word says
 // so); the int64-position path answers what is left.  OUT_SPAN -- int32
 // position - answer (position + 1 for none): the stock span, with the flip.
+// REV (single arrays, no view head, 4-byte keys): the run sees the array
+// reversed -- tile t holds elements n - 1 - (t * WT + e), its TMA rows counted
+// from the end (n a multiple of 32) and reversed in shared memory as they
+// land -- and writes each answer mirrored back, n - 1 - answer (-1 for none)
+// at element n - 1 - position: the next smaller key, in one run.
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32,
+          bool REV = false>
 __global__ void __launch_bounds__(WPC * 32, (WPC >= 16 && sizeof(T) == 4 ? 1 : 2))
 apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_constant__ CUtensorMap map_out,
                  const RangeArgs a) {
@@ -449,12 +462,14 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
     };
     auto seg_idx = [&](int pos) { return a.offsets ? seg_find(a.offsets, a.nseg, pos, err) : 0; };
     static_assert(OUTM == OUT_I32 || (!SEG && EP), "int64 and span answers: single arrays only");
+    static_assert(!REV || (!SEG && EP && OUTM == OUT_I32 && KB == 4), "reversed runs: single arrays of 4-byte keys");
     constexpr bool OUT64 = OUTM == OUT_I64;
     // a final answer v of position pos (phase 2); int64 answers: out_base + v, and
     // UNRESOLVED64 for none (the key is left to the int64-position path); spans:
     // pos - v
     auto put = [&](int pos, int v) {
         if constexpr (OUT64) a.d_out64[pos] = v >= 0 ? (int64_t)v + a.out_base : UNRESOLVED64;
+        else if constexpr (REV) a.d_out[a.n - 1 - pos] = v >= 0 ? a.n - 1 - v : -1;
         else if constexpr (OUTM == OUT_SPAN) a.d_out[pos] = pos - v;
         else a.d_out[pos] = v;
     };
@@ -482,11 +497,13 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         const int t1 = min(t0 + a.tiles_per_range, a.num_tiles);
         const int ntr = t1 - t0;
         auto tile_full = [&](int t) { return a.tma_rows > 0 && (t + 1) * RPT <= a.tma_rows && (t > 0 || head == 0); };
+        // the first TMA row of tile t (reversed runs: counted from the end)
+        auto tile_row = [&](int t) { return REV ? a.tma_rows - (t + 1) * RPT : t * RPT; };
         if (lane == 0) {
             for (int i = 0; i < kStages && i < ntr; i++)
                 if (tile_full(t0 + i)) {
                     mbar_arrive_expect_tx(&bar[i], (uint32_t)(WT * KB));
-                    tma_load_2d(sV + (size_t)i * WT, &map_in, 0, (t0 + i) * RPT, &bar[i]);
+                    tma_load_2d(sV + (size_t)i * WT, &map_in, 0, tile_row(t0 + i), &bar[i]);
                 }
         }
         // Range state (warp-uniform): the stack ring [stk_lo, stk_hi) of strict
@@ -525,6 +542,15 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 
             if (full) {
                 if (!mbar_wait_bounded(&bar[slot], par, a.spin_limit) && lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+                if constexpr (REV) {  // the tile arrived in element order: reverse it in place
+                    T rv[IPT];
+#pragma unroll
+                    for (int j = 0; j < IPT; j++) rv[j] = V[ks(WT - 1 - (j * 32 + lane))];
+                    __syncwarp();
+#pragma unroll
+                    for (int j = 0; j < IPT; j++) V[ks(j * 32 + lane)] = rv[j];
+                    __syncwarp();
+                }
                 if constexpr (MAPF != KMAP_NONE) {  // the tile's keys through the key map, in place
 #pragma unroll
                     for (int j = 0; j < IPT; j++) {
@@ -537,7 +563,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 for (int j = 0; j < IPT; j++) {
                     const int e = j * 32 + lane;
                     const int g = tile_base + e;
-                    V[ks(e)] = g < a.n && (!head || g >= head) ? (MAPF != KMAP_NONE ? load_key<T, MAPF>(&d_in[g]) : d_in[g])
+                    V[ks(e)] = g < a.n && (!head || g >= head) ? (MAPF != KMAP_NONE || REV ? key_at<T, MAPF, REV>(d_in, a.n, g) : d_in[g])
                                                                 : KeyTraits<T>::pad();
                 }
                 // A view head makes tile 0 plain while tile kStages streams into its
@@ -675,6 +701,36 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     }
                     return;
                 }
+                if constexpr (REV) {  // mirrored answers at the mirrored positions, in element order
+                    __syncwarp();     // every lane's answers are in O
+                    if (full) {
+                        int ro[IPT];
+#pragma unroll
+                        for (int j = 0; j < IPT; j++) {
+                            const int o = O[swz(WT - 1 - (j * 32 + lane))];
+                            ro[j] = o >= 0 ? a.n - 1 - o : -1;
+                        }
+                        __syncwarp();
+#pragma unroll
+                        for (int j = 0; j < IPT; j++) O[swz(j * 32 + lane)] = ro[j];
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            tma_store_2d(&map_out, 0, tile_row(t), O);
+                            bulk_commit();
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < IPT; j++) {
+                            const int e = j * 32 + lane;
+                            if (e < valid_keys) {
+                                const int o = O[swz(e)];
+                                a.d_out[a.n - 1 - (tile_base + e)] = o >= 0 ? a.n - 1 - o : -1;
+                            }
+                        }
+                    }
+                    return;
+                }
                 if constexpr (OUTM == OUT_SPAN) {  // spans: position - answer
                     __syncwarp();                   // every lane's answers are in O
     #pragma unroll
@@ -774,7 +830,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         __stcg(&tile_min_w[t], tmin);
                     }
                     def_total += WT;
-                    if constexpr (OUTM == OUT_SPAN) {
+                    if constexpr (OUTM == OUT_SPAN || REV) {
                         store_tile();
                     } else if constexpr (!OUT64) {  // (int64 answers: the tile is left to the int64-position path)
                         fence_proxy_async_smem();
@@ -800,7 +856,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     __syncwarp();
                     if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
                         mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * KB));
-                        tma_load_2d(V, &map_in, 0, (t + kStages) * RPT, &bar[slot]);
+                        tma_load_2d(V, &map_in, 0, tile_row(t + kStages), &bar[slot]);
                     }
                     continue;
                 }
@@ -840,7 +896,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         __stcg(&a.s.tile_flag[t], 0u);
                         __stcg(&tile_min_w[t], first);
                     }
-                    if constexpr (OUTM != OUT_I32) {
+                    if constexpr (OUTM != OUT_I32 || REV) {
                         store_tile();
                     } else {
                         fence_proxy_async_smem();
@@ -871,7 +927,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     __syncwarp();
                     if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
                         mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * KB));
-                        tma_load_2d(V, &map_in, 0, (t + kStages) * RPT, &bar[slot]);
+                        tma_load_2d(V, &map_in, 0, tile_row(t + kStages), &bar[slot]);
                     }
                     continue;
                 }
@@ -1316,7 +1372,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
             __syncwarp();
             if (lane == 0 && i + kStages < ntr && tile_full(t + kStages)) {
                 mbar_arrive_expect_tx(&bar[slot], (uint32_t)(WT * KB));
-                tma_load_2d(V, &map_in, 0, (t + kStages) * RPT, &bar[slot]);
+                tma_load_2d(V, &map_in, 0, tile_row(t + kStages), &bar[slot]);
             }
         }
 
@@ -1425,7 +1481,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                 const T qf = __shfl_sync(FULL, q, f);
                 const int rpf = __shfl_sync(FULL, rp, f);
                 const int lim = rpf >= 0 ? range_end(rpf) : range_begin;
-                const int found = find_left<T, WT, INCL, MAPF>(qf, lim, d_in, tile_min_r, chunk_min_r, a);
+                const int found = find_left<T, WT, INCL, MAPF, REV>(qf, lim, d_in, tile_min_r, chunk_min_r, a);
                 if (lane == f) ans = found;
             }
             if (want) {
@@ -1495,7 +1551,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                     const uint32_t mw = __shfl_sync(FULL, mwl, w);
                     const int pos = t * WT + w * 32 + lane;
                     const bool pk = ((mw >> lane) & 1u) && pos >= from && (!head || pos >= head);
-                    sV[w * 32 + lane] = pk ? load_key<T, MAPF>(&d_in[pos]) : KeyTraits<T>::pad();
+                    sV[w * 32 + lane] = pk ? key_at<T, MAPF, REV>(d_in, a.n, pos) : KeyTraits<T>::pad();
                 }
                 for (int w = 0; w < W && !a_done; w++) {
                     const uint32_t mw = __shfl_sync(FULL, mwl, w);
@@ -1508,7 +1564,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             const int f = __ffs(pend) - 1;
                             pend &= pend - 1;
                             const int pf = t * WT + w * 32 + f;
-                            const int found = find_left<T, WT, INCL, MAPF>(__shfl_sync(FULL, q, f), pf, d_in, tile_min_r,
+                            const int found = find_left<T, WT, INCL, MAPF, REV>(__shfl_sync(FULL, q, f), pf, d_in, tile_min_r,
                                                                      chunk_min_r, a);
                             int sf = 0;
                             if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
@@ -1550,7 +1606,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                                                           : KeyTraits<T>::pad();
                                 const unsigned m = __ballot_sync(FULL, lane < cnt && lt<INCL>(tkey, qf));
                                 found = m ? __ldcg(&a.s.top_pos[(size_t)rpf * kTopEntries + 31 - __clz(m)])
-                                          : find_left<T, WT, INCL, MAPF>(qf, range_end(rpf), d_in, tile_min_r, chunk_min_r, a);
+                                          : find_left<T, WT, INCL, MAPF, REV>(qf, range_end(rpf), d_in, tile_min_r, chunk_min_r, a);
                             }
                         }
                         if (found < 0) {
@@ -1559,7 +1615,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                             a_done = true;
                         } else {
                             cur = found;
-                            cv = load_key<T, MAPF>(&d_in[cur]);
+                            cv = key_at<T, MAPF, REV>(d_in, a.n, cur);
                         }
                     }
                 }
@@ -1571,7 +1627,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
         const int ncap = min(cap_total, kCapCap);
         for (int j = 0; j < ncap; j++) {
             const int pos = sCapP[j];
-            const int found = find_left<T, WT, INCL, MAPF>(load_key<T, MAPF>(&d_in[pos]), pos, d_in, tile_min_r,
+            const int found = find_left<T, WT, INCL, MAPF, REV>(key_at<T, MAPF, REV>(d_in, a.n, pos), pos, d_in, tile_min_r,
                                                            chunk_min_r, a);
             if (lane == 0) {
                 if (found < 0) atomicOr(err, ERR_INTERNAL);
@@ -1598,7 +1654,7 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
                         pend &= pend - 1;
                         const int pf = t * WT + w * 32 + f;
                         const int found =
-                            find_left<T, WT, INCL, MAPF>(load_key<T, MAPF>(&d_in[pf]), pf, d_in, tile_min_r, chunk_min_r, a);
+                            find_left<T, WT, INCL, MAPF, REV>(key_at<T, MAPF, REV>(d_in, a.n, pf), pf, d_in, tile_min_r, chunk_min_r, a);
                         int sf = 0;
                         if constexpr (SEG) sf = (int)seg_off(seg_idx(pf - head)) + head;
                         if (lane == f) {
@@ -1638,7 +1694,8 @@ apse_warp_kernel(const __grid_constant__ CUtensorMap map_in, const __grid_consta
 // ---------------------------------------------------------------------------
 // Launch plumbing shared by the single-array and segmented translation units.
 // ---------------------------------------------------------------------------
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32,
+          bool REV = false>
 inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorMap& mo, cudaStream_t st,
                             int max_warps) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
@@ -1647,14 +1704,15 @@ inline cudaError_t launch_t(RangeArgs& a, const CUtensorMap& mi, const CUtensorM
     a.tiles_per_range = tpr;
     a.num_ranges = (a.num_tiles + tpr - 1) / tpr;
     const int ctas = (a.num_ranges + WPC - 1) / WPC;
-    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUTM><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
+    apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUTM, REV><<<ctas, WPC * 32, smem, st>>>(mi, mo, a);
     return cudaGetLastError();
 }
 
-template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32>
+template <typename T, int IPT, int WPC, bool INCL, bool SEG, bool EP, int MAPF = KMAP_NONE, int OUTM = OUT_I32,
+          bool REV = false>
 inline cudaError_t prepare_t(int* ctas_per_sm) {
     constexpr size_t smem = kernel_smem_bytes<IPT, WPC, (int)sizeof(T)>();
-    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUTM>;
+    auto k = apse_warp_kernel<T, IPT, WPC, INCL, SEG, EP, MAPF, OUTM, REV>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int n = 0;

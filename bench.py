@@ -342,10 +342,13 @@ def run_consumers(dev, peak_gbs: float) -> dict:
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ops = {  # name: (call, caller bytes per key, pass bytes per key)
         "prev_greater": (lambda: consumers.prev_greater(x, plan=plan, work=work), 8, 8),  # one flipped run
-        "next_smaller": (lambda: consumers.next_smaller(x, plan=plan, work=work), 8, 24),
+        "next_smaller": (lambda: consumers.next_smaller(x, plan=plan, work=work), 8, 8),  # one reversed run
         "stock_span": (lambda: consumers.stock_span(x, plan=plan, work=work), 8, 8),  # flipped run, span out
-        "cartesian_parents": (lambda: consumers.cartesian_parents(x, plan=plan, work=work), 8, 40),
-        "largest_rectangle": (lambda: consumers.largest_rectangle(h, plan=plan, work=work), 4, 36),
+        # two runs (forward, reversed) of 8 B a key, then the parent pass: L, R, the
+        # two keys compared (gathers) and the answer, 20 B
+        "cartesian_parents": (lambda: consumers.cartesian_parents(x, plan=plan, work=work), 8, 36),
+        # two runs of 8 B a key, then the area pass over h, L and R, 12 B
+        "largest_rectangle": (lambda: consumers.largest_rectangle(h, plan=plan, work=work), 4, 28),
     }
     res = {}
     for name, (call, ub, pb) in ops.items():

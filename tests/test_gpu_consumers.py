@@ -151,3 +151,25 @@ def test_flipped_run_and_its_general_route(plans, dtype, shift):
                   "prev_greater %s %s" % (name, le))
         check(consumers.stock_span(x, plan=plan).cpu().numpy(), oc.stock_span(a), "stock_span %s" % name)
     plan.check()
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.float32])
+@pytest.mark.parametrize("name", ["uniform", "dup16", "desc", "asc"])
+def test_reversed_run(plans, dtype, name):
+    # n a multiple of 32 on a 16-byte boundary: next smaller is one engine run
+    # over the reversed array (TMA tiles counted from the end, a partial tile
+    # at the array's start when n is not a multiple of 512; below 512 keys
+    # plain loads), and the histogram and the Cartesian tree use it
+    rng = np.random.default_rng(70 + sum(map(ord, name)))
+    plan = plans[dtype]
+    for n in (32, 480, 512, 544, 4096, 65536, 1_000_032, 2_000_032):
+        a = keys(name, n, rng, dtype)
+        x = torch.from_numpy(a).cuda()
+        for le in (False, True):
+            check(consumers.next_smaller(x, le, plan=plan).cpu().numpy(), oc.next_smaller(a, le),
+                  "next_smaller %s %d" % (le, n))
+        check(consumers.cartesian_parents(x, plan=plan).cpu().numpy(), oc.cartesian_parents(a), "cartesian %d" % n)
+        if dtype == np.int32:
+            h = (np.abs(a.astype(np.int64)) % (1 << 20)).astype(np.int32)
+            assert consumers.largest_rectangle(torch.from_numpy(h).cuda(), plan=plan) == oc.largest_rectangle(h), n
+    plan.check()
