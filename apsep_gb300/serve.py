@@ -193,9 +193,10 @@ class PoolServer:
     copies overlap this batch's run, and the lanes of both kinds run side by
     side.  When a lane's batch completes its requests are done and their
     ring spans are released.  Size classes: a request of at least
-    direct_min_keys keys whose keys and output are both device memory on a
-    16-byte boundary is not copied at all: it runs in place on a lane as a
-    single-array launch.  After every launch the lane enqueues a copy of its
+    direct_min_keys keys whose keys are device memory on a 16-byte boundary
+    is not copied at all: it runs from its own keys on a lane as a
+    single-array launch, into its device output (on a 16-byte boundary) or,
+    with out None, into a span of the answer ring.  After every launch the lane enqueues a copy of its
     plan's error word; a batch whose word is nonzero is marked failed when it
     retires (and the plan re-armed), so an error is tied to its requests."""
 
@@ -236,17 +237,21 @@ class PoolServer:
                 ln.plan.close()
 
     def _direct(self, r: Request) -> bool:
+        # device keys on a 16-byte boundary; answers to a device out on one, or
+        # (out None) into the answer ring
         return (self.direct_min_keys is not None and r.n >= self.direct_min_keys and r.keys.is_cuda
-                and r.out is not None and r.out.is_cuda and r.keys.data_ptr() % 16 == 0
-                and r.out.data_ptr() % 16 == 0 and r.n <= self.max_batch_keys)
+                and r.keys.data_ptr() % 16 == 0 and r.n <= self.max_batch_keys
+                and ((r.out is None and r.n <= self.ring_keys) or
+                     (r.out is not None and r.out.is_cuda and r.out.data_ptr() % 16 == 0)))
 
     def _finish_launch(self, ln: _Lane) -> None:
         ln.plan.error_async(ln.err_host, stream=ln.stream)
         ln.event.record(ln.stream)
 
-    def _launch_direct(self, ln: _Lane, r: Request) -> None:
+    def _launch_direct(self, kind, ln: _Lane, r: Request) -> None:
         ln.batch = [r]
-        ln.plan.run(r.keys, out=r.out[:r.n], n=r.n, stream=ln.stream)
+        out = r.out[:r.n] if r.out is not None else self.rings[kind][1][r.slot:r.slot + r.n]
+        ln.plan.run(r.keys, out=out, n=r.n, stream=ln.stream)
         self._finish_launch(ln)
 
     def _launch_batch(self, kind, ln: _Lane, batch: list, copied: torch.cuda.Event) -> None:
@@ -314,8 +319,13 @@ class PoolServer:
                 idle = [ln for ln in self.lanes[k] if not ln.batch]
                 if not idle:
                     break
+                if r.out is None:  # its answers take a ring span (its keys stay where they are)
+                    start = ring.alloc(r._n)
+                    if start is None:
+                        break
+                    r.slot = start
                 waiting.popleft()
-                self._launch_direct(idle[0], r)
+                self._launch_direct(k, idle[0], r)
                 self._nbatches += 1
                 return True
             start = ring.alloc(r._n)

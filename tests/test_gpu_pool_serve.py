@@ -123,3 +123,26 @@ def test_copy_spans_every_alignment_and_size():
     s2 = src.cpu().numpy()
     for i in range(600):
         assert np.array_equal(h[i, :61], s2[64 * i + 3:64 * i + 64])
+
+
+def test_direct_runs_answer_into_the_ring():
+    """Large requests run from their own keys (no copy into the pool); with no
+    output buffer their answers land in a span of the answer ring, handed to
+    on_done, while the small ones are batched around them."""
+    reqs = pool_requests(32, rate=0.0, seed=35, hi=1 << 22)
+    for r in reqs:
+        r.out = None
+    got = {}
+
+    def done(r, answers):
+        got[r.rid] = answers.cpu().numpy()
+
+    srv = PoolServer(budget_bytes=1 << 30, max_batch_keys=1 << 22, ring_keys=5 << 20, direct_min_keys=1 << 20)
+    try:
+        st = srv.serve(reqs, realtime=False, on_done=done)
+    finally:
+        srv.close()
+    assert st.requests == 32 and any(r.n >= 1 << 20 for r in reqs) and any(r.n < 1 << 20 for r in reqs)
+    for r in reqs:
+        assert not r.failed
+        assert np.array_equal(got[r.rid], oracle.apse(host_keys(r))), r.rid
