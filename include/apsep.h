@@ -176,9 +176,11 @@ apsep_status apsep_noalloc_check(void* stream);
 
 /* ---- Consumers of APSE ------------------------------------------------------
  * The classic callers the reference names for its output (README.md:3,
- * src/bench_spt_le.cu:1-3), each a few memory-bound passes around one or two
- * runs on `plan` (whose key type they use; n <= its capacity), asynchronous
- * on `stream` like apsep_run.  d_work: a 16-byte aligned device workspace of
+ * src/bench_spt_le.cu:1-3), each one or two runs on `plan` (whose key type
+ * they use; n <= its capacity) -- with 4-byte keys and 16-byte aligned keys
+ * and answers the engine flips or reverses the keys as it loads them (next
+ * smaller: n a multiple of 32), else memory-bound flip / reverse / mirror
+ * passes around plain runs -- asynchronous on `stream` like apsep_run.  d_work: a 16-byte aligned device workspace of
  * apsep_consumer_workspace_bytes(n) bytes, not overlapping the inputs or
  * outputs.  Device-side errors of the inner runs surface through
  * apsep_plan_check. */
@@ -220,9 +222,9 @@ apsep_status apsep_cartesian_parents(apsep_plan* plan, const void* d_in, int32_t
  * (src/apsep.cuh:3052-3076) while its key types anticipate longer arrays
  * (src/apsep.cuh:62-70).  The array runs as consecutive pieces of the plan's
  * capacity (rounded down to whole 32-key groups; the whole array when
- * n <= capacity), one engine run each; keys that no key of their own piece
- * answers are answered from a hierarchy of minima over the keys before the
- * piece.  d_work: a 16-byte aligned device workspace of
+ * n <= capacity), one engine run each writing b0 + answer as int64; keys
+ * that no key of their own piece answers are answered from a hierarchy of
+ * minima over the keys before the piece.  d_work: a 16-byte aligned device workspace of
  * apsep_run64_workspace_bytes(plan, n) bytes (-1: n out of range, or a plan
  * with capacity < 32 for n > capacity), not overlapping the keys or d_out
  * (8-byte aligned).  Asynchronous on `stream` and graph-capturable like
