@@ -302,7 +302,9 @@ apsep_status plan_run_flipped(apsep_plan* p, const void* d_in, int32_t* d_out, i
     if (!p || n <= 0 || n > p->capacity || !d_in || !d_out || (cmp != APSEP_LT && cmp != APSEP_LE)) return APSEP_EINVAL;
     if (wide(p->dtype) || (span && cmp != APSEP_LT)) return APSEP_ENOTSUP;
     if ((uintptr_t)d_in % 4 != 0 || (uintptr_t)d_out % 4 != 0) return APSEP_EINVAL;
-    if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_EINVAL;
+    // answers over the keys themselves (in place) take the general route, which
+    // reads the keys into the workspace first
+    if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_ENOTSUP;
     // a view head would need the view instantiation: those runs take the general route
     if ((uintptr_t)d_in % 16 != (uintptr_t)d_out % 16 || (uintptr_t)d_in % 16 != 0) return APSEP_ENOTSUP;
     DeviceGuard g(p->device);
@@ -342,7 +344,7 @@ apsep_status plan_run_reversed(apsep_plan* p, const void* d_in, int32_t* d_out, 
     if (!p || n <= 0 || n > p->capacity || !d_in || !d_out || (cmp != APSEP_LT && cmp != APSEP_LE)) return APSEP_EINVAL;
     if (wide(p->dtype) || n % 32 != 0) return APSEP_ENOTSUP;
     if ((uintptr_t)d_in % 16 != 0 || (uintptr_t)d_out % 16 != 0) return APSEP_ENOTSUP;
-    if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_EINVAL;
+    if (ranges_overlap(d_in, (size_t)n * 4, d_out, (size_t)n * 4)) return APSEP_ENOTSUP;  // in place: general route
     DeviceGuard g(p->device);
     if (!g.ok) return APSEP_ECUDA;
     const int B = 32 * kTileConfigs[0].ipt;  // keys per warp tile

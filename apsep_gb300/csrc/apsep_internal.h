@@ -196,15 +196,15 @@ struct apsep_plan;
 // One single-array run of the plan through the order-reversing key map
 // (launch_range_flipped): previous greater (span = 0) or the stock span
 // (span = 1, APSEP_LT).  APSEP_ENOTSUP when the engine has no such form for
-// the call (8-byte keys, or keys and answers at different 16-byte phases):
-// the caller then takes its general route.
+// the call (8-byte keys, keys or answers off a 16-byte boundary, answers over
+// the keys): the caller then takes its general route.
 apsep_status plan_run_flipped(struct apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
                               int span, void* stream);
 // One single-array run of the plan over the reversed array
 // (launch_range_reversed): out[i] = the next j > i with a[j] < a[i] (<= under
 // APSEP_LE), else -1.  APSEP_ENOTSUP when the engine has no such form for the
 // call (8-byte keys, keys or answers off a 16-byte boundary, n not a multiple
-// of 32): the caller then takes its general route.
+// of 32, answers over the keys): the caller then takes its general route.
 apsep_status plan_run_reversed(struct apsep_plan* plan, const void* d_in, int32_t* d_out, int64_t n, apsep_cmp cmp,
                                void* stream);
 apsep_status plan_run_out64(struct apsep_plan* plan, const void* d_in, int64_t* d_out, int64_t n, int64_t out_base,

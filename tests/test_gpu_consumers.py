@@ -173,3 +173,26 @@ def test_reversed_run(plans, dtype, name):
             h = (np.abs(a.astype(np.int64)) % (1 << 20)).astype(np.int32)
             assert consumers.largest_rectangle(torch.from_numpy(h).cuda(), plan=plan) == oc.largest_rectangle(h), n
     plan.check()
+
+
+def test_answers_over_the_keys_through_the_c_abi(plans):
+    # d_out == d_in: the one-run forms step aside (the engine cannot read keys
+    # it is overwriting) and the workspace route answers in place
+    lib = _lib.load()
+    vp = ctypes.c_void_p
+    plan = plans[np.int32]
+    rng = np.random.default_rng(88)
+    n = 65536
+    a = rng.integers(-1000, 1000, n).astype(np.int32)
+    w = torch.empty(consumers.workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    for fn, want in (("apsep_run_prev_greater", oc.prev_greater(a, False)),
+                     ("apsep_run_next_smaller", oc.next_smaller(a, False)),
+                     ("apsep_stock_span", oc.stock_span(a))):
+        buf = torch.from_numpy(a.copy()).cuda()
+        args = [plan._h, vp(buf.data_ptr()), vp(buf.data_ptr()), n]
+        if fn != "apsep_stock_span":
+            args.append(_lib.LT)
+        assert getattr(lib, fn)(*args, vp(w.data_ptr()), None) == _lib.APSEP_OK, fn
+        torch.cuda.synchronize()
+        check(buf.cpu().numpy(), want, fn + " in place")
+    plan.check()
